@@ -1,0 +1,352 @@
+"""axom_gb300: GB300-native spatial queries (axom spin::BVH + quest::SignedDistance).
+
+Python mirror of the reference interface over the C ABI in ``include/gsq.h``
+(``libgsq.so``, built by ``axom_gb300.build``).  Class and method names follow
+the reference:
+
+* ``BVH``            -- ``spin::BVH<3, Exec, double>`` (spin/BVH.hpp:129-568):
+  ``initialize``, ``find_points``, ``find_rays``, ``find_bounding_boxes``,
+  ``get_bounds``, ``set/get_scale_factor``, ``set/get_tolerance``.
+* ``SignedDistance`` -- ``quest::SignedDistance<3, Exec>``
+  (quest/SignedDistance.hpp:147-605): ``compute_distance``,
+  ``compute_distances``, ``get_mesh_bounds``, ``get_bvh_tree``.
+
+Arrays may be numpy arrays (host memory) or torch tensors (host or CUDA); the
+C ABI classifies each pointer.  Outputs are numpy arrays for host inputs and
+torch CUDA tensors for device inputs.  There is no CPU fallback: without the
+compiled library or a CUDA device every call raises.
+"""
+from __future__ import annotations
+
+import ctypes as C
+from pathlib import Path
+
+import numpy as np
+
+__all__ = ["GsqError", "BVH", "SignedDistance", "load", "PRECISION_FP64", "PRECISION_MIXED"]
+
+PKG = Path(__file__).resolve().parent
+LIB_PATH = PKG / "libgsq.so"
+
+GSQ_OK = 0
+BVH_BUILD_OK = 0
+PRECISION_FP64 = 0
+PRECISION_MIXED = 1
+DEFAULT_SCALE_FACTOR = 1.000123
+DEFAULT_TOLERANCE = float(np.finfo(np.float64).eps)
+
+_lib = None
+_vp, _dp, _ip, _up = C.c_void_p, C.POINTER(C.c_double), C.POINTER(C.c_int32), C.POINTER(C.c_uint32)
+_i64p = C.POINTER(C.c_int64)
+
+
+class GsqError(RuntimeError):
+    def __init__(self, code: int, msg: str):
+        super().__init__(f"gsq error {code}: {msg}")
+        self.code = code
+
+
+class SdfOpts(C.Structure):
+    _fields_ = [("precision", C.c_int32), ("sort_queries", C.c_int32), ("block_size", C.c_int32),
+                ("reserved", C.c_int32 * 5)]
+
+
+# (name, restype, argtypes) of every entry point declared in include/gsq.h
+SIGNATURES = [
+    ("gsq_last_error", C.c_char_p, []),
+    ("gsq_version", C.c_char_p, []),
+    ("gsq_kernel_launches", C.c_int64, []),
+    ("gsq_free", C.c_int, [_vp]),
+    ("gsq_memcpy", C.c_int, [_vp, _vp, C.c_size_t]),
+    ("gsq_bvh_create", C.c_int, [C.POINTER(_vp)]),
+    ("gsq_bvh_destroy", C.c_int, [_vp]),
+    ("gsq_bvh_set_scale_factor", C.c_int, [_vp, C.c_double]),
+    ("gsq_bvh_get_scale_factor", C.c_int, [_vp, _dp]),
+    ("gsq_bvh_set_tolerance", C.c_int, [_vp, C.c_double]),
+    ("gsq_bvh_get_tolerance", C.c_int, [_vp, _dp]),
+    ("gsq_bvh_build", C.c_int, [_vp, _vp, C.c_int32, _vp]),
+    ("gsq_bvh_bounds", C.c_int, [_vp, _dp, _dp]),
+    ("gsq_bvh_num_leaves", C.c_int, [_vp, _ip]),
+    ("gsq_bvh_find_boxes", C.c_int, [_vp, _vp, C.c_int32, _vp, _vp, C.POINTER(_vp), _i64p, _vp]),
+    ("gsq_bvh_find_points", C.c_int, [_vp, _vp, C.c_int32, _vp, _vp, C.POINTER(_vp), _i64p, _vp]),
+    ("gsq_bvh_find_rays", C.c_int, [_vp, _vp, _vp, C.c_int32, _vp, _vp, C.POINTER(_vp), _i64p, _vp]),
+    ("gsq_ray_normalize", C.c_int, [_dp, C.c_int32, _dp]),
+    ("gsq_bvh_export", C.c_int, [_vp, _dp, _ip, _ip, _up]),
+    ("gsq_bvh_last_build_ms", C.c_int, [_vp, C.POINTER(C.c_float)]),
+    ("gsq_sdf_opts_init", C.c_int, [C.POINTER(SdfOpts)]),
+    ("gsq_sdf_create", C.c_int, [C.POINTER(_vp), _vp, _vp, _vp, C.c_int32, _vp, C.c_int32, C.c_int32, C.c_int32,
+                                 C.c_int32, C.POINTER(SdfOpts), _vp]),
+    ("gsq_sdf_destroy", C.c_int, [_vp]),
+    ("gsq_sdf_set_opts", C.c_int, [_vp, C.POINTER(SdfOpts)]),
+    ("gsq_sdf_eval", C.c_int, [_vp, _vp, _vp, _vp, C.c_int32, C.c_int32, _vp, _vp, _vp, _vp]),
+    ("gsq_sdf_mesh_bounds", C.c_int, [_vp, _dp, _dp]),
+    ("gsq_sdf_get_bvh", C.c_int, [_vp, C.POINTER(_vp)]),
+    ("gsq_sdf_last_eval_ms", C.c_int, [_vp, C.POINTER(C.c_float)]),
+]
+
+
+def load(path: Path | str | None = None) -> C.CDLL:
+    """Loads libgsq.so (raises if it has not been built)."""
+    global _lib
+    if _lib is not None and path is None:
+        return _lib
+    p = Path(path) if path else LIB_PATH
+    if not p.exists():
+        raise FileNotFoundError(f"{p} is missing: run axom_gb300.build.build() (no CPU fallback exists)")
+    lib = C.CDLL(str(p))
+    for name, res, args in SIGNATURES:
+        f = getattr(lib, name)
+        f.restype, f.argtypes = res, args
+    if path is None:
+        _lib = lib
+    return lib
+
+
+def _check(rc: int):
+    if rc != GSQ_OK:
+        raise GsqError(rc, load().gsq_last_error().decode())
+
+
+# ---- array plumbing -----------------------------------------------------------
+def _is_torch(a) -> bool:
+    return type(a).__module__.startswith("torch")
+
+
+def _stream():
+    try:
+        import torch
+        if torch.cuda.is_available() and torch.cuda.is_initialized():
+            return C.c_void_p(torch.cuda.current_stream().cuda_stream)
+    except ImportError:
+        pass
+    return None
+
+
+class _Arr:
+    """A contiguous array view with a raw pointer (host numpy or torch)."""
+
+    def __init__(self, a, dtype, cols=None):
+        if _is_torch(a):
+            import torch
+            tdt = {np.float64: torch.float64, np.int32: torch.int32}[dtype]
+            t = a.to(tdt).contiguous()
+            if cols:
+                t = t.reshape(-1, cols)
+            self.obj, self.ptr, self.device = t, t.data_ptr(), t.is_cuda
+            self.n = t.shape[0] if t.dim() else 1
+            self.torch_device = t.device
+        else:
+            x = np.ascontiguousarray(a, dtype=dtype)
+            if cols:
+                x = x.reshape(-1, cols)
+            self.obj, self.ptr, self.device = x, x.ctypes.data, False
+            self.n = x.shape[0] if x.ndim else 1
+            self.torch_device = None
+
+    def empty(self, shape, dtype):
+        if self.device:
+            import torch
+            tdt = {np.float64: torch.float64, np.int32: torch.int32}[dtype]
+            return torch.empty(shape, dtype=tdt, device=self.torch_device)
+        return np.empty(shape, dtype=dtype)
+
+
+def _ptr(a):
+    return a.data_ptr() if _is_torch(a) else a.ctypes.data
+
+
+class BVH:
+    """spin::BVH<3, CUDA_EXEC, double> on the GB300 (spin/BVH.hpp:129-568)."""
+
+    def __init__(self, boxes=None, num_items: int | None = None, scale_factor: float = DEFAULT_SCALE_FACTOR,
+                 tolerance: float = DEFAULT_TOLERANCE, _handle=None):
+        self._lib = load()
+        self._owned = _handle is None
+        if _handle is None:
+            h = _vp()
+            _check(self._lib.gsq_bvh_create(C.byref(h)))
+            self._h = h
+            self.set_scale_factor(scale_factor)
+            self.set_tolerance(tolerance)
+        else:
+            self._h = _handle
+        if boxes is not None:
+            self.initialize(boxes, num_items)
+
+    def __del__(self):
+        if getattr(self, "_owned", False) and getattr(self, "_h", None):
+            self._lib.gsq_bvh_destroy(self._h)
+            self._h = None
+
+    def set_scale_factor(self, s: float):
+        _check(self._lib.gsq_bvh_set_scale_factor(self._h, s))
+
+    def get_scale_factor(self) -> float:
+        v = C.c_double()
+        _check(self._lib.gsq_bvh_get_scale_factor(self._h, C.byref(v)))
+        return v.value
+
+    def set_tolerance(self, t: float):
+        _check(self._lib.gsq_bvh_set_tolerance(self._h, t))
+
+    def get_tolerance(self) -> float:
+        v = C.c_double()
+        _check(self._lib.gsq_bvh_get_tolerance(self._h, C.byref(v)))
+        return v.value
+
+    def initialize(self, boxes, num_items: int | None = None) -> int:
+        """Builds over (n, 6) boxes [xmin, ymin, zmin, xmax, ymax, zmax]."""
+        b = _Arr(boxes, np.float64, 6)
+        n = b.n if num_items is None else int(num_items)
+        _check(self._lib.gsq_bvh_build(self._h, C.c_void_p(b.ptr), n, _stream()))
+        return BVH_BUILD_OK
+
+    def get_bounds(self):
+        lo, hi = np.empty(3), np.empty(3)
+        _check(self._lib.gsq_bvh_bounds(self._h, lo.ctypes.data_as(_dp), hi.ctypes.data_as(_dp)))
+        return lo, hi
+
+    def num_leaves(self) -> int:
+        v = C.c_int32()
+        _check(self._lib.gsq_bvh_num_leaves(self._h, C.byref(v)))
+        return v.value
+
+    def last_build_ms(self) -> float:
+        v = C.c_float()
+        _check(self._lib.gsq_bvh_last_build_ms(self._h, C.byref(v)))
+        return v.value
+
+    def _find(self, fn, arrs, m, like: _Arr):
+        off = like.empty(m, np.int32)
+        cnt = like.empty(m, np.int32)
+        cand = _vp()
+        total = C.c_int64()
+        _check(fn(self._h, *[C.c_void_p(a.ptr) for a in arrs], m, C.c_void_p(_ptr(off)), C.c_void_p(_ptr(cnt)),
+                  C.byref(cand), C.byref(total), _stream()))
+        t = total.value
+        try:
+            if like.device:
+                import torch
+                out = torch.empty(t, dtype=torch.int32, device=like.torch_device)
+                if t:
+                    _check(self._lib.gsq_memcpy(C.c_void_p(out.data_ptr()), cand, C.c_size_t(4 * t)))
+            else:
+                out = np.ctypeslib.as_array(C.cast(cand, _ip), shape=(max(t, 1),))[:t].copy() if t else \
+                    np.empty(0, np.int32)
+        finally:
+            self._lib.gsq_free(cand)
+        return off, cnt, out
+
+    def find_bounding_boxes(self, boxes):
+        """(offsets, counts, candidates) for (m, 6) query boxes."""
+        q = _Arr(boxes, np.float64, 6)
+        return self._find(self._lib.gsq_bvh_find_boxes, [q], q.n, q)
+
+    def find_points(self, points):
+        q = _Arr(points, np.float64, 3)
+        return self._find(self._lib.gsq_bvh_find_points, [q], q.n, q)
+
+    def find_rays(self, origins, directions):
+        """Rays with stored unit directions (see normalize_rays)."""
+        o = _Arr(origins, np.float64, 3)
+        d = _Arr(directions, np.float64, 3)
+        return self._find(self._lib.gsq_bvh_find_rays, [o, d], o.n, o)
+
+    def export(self):
+        """Reference LinearBVH layout: (node_boxes, children, leaf_ids, codes)."""
+        n = self.num_leaves()
+        nodes = np.empty((2 * (n - 1), 6))
+        ch = np.empty(2 * (n - 1), np.int32)
+        leaf = np.empty(n, np.int32)
+        codes = np.empty(n, np.uint32)
+        _check(self._lib.gsq_bvh_export(self._h, nodes.ctypes.data_as(_dp), ch.ctypes.data_as(_ip),
+                                        leaf.ctypes.data_as(_ip), codes.ctypes.data_as(_up)))
+        return nodes, ch, leaf, codes
+
+
+def normalize_rays(directions) -> np.ndarray:
+    """primal::Ray's direction normalisation (Vector::unitVector) on the host."""
+    d = np.ascontiguousarray(directions, dtype=np.float64).reshape(-1, 3)
+    out = np.empty_like(d)
+    _check(load().gsq_ray_normalize(d.ctypes.data_as(_dp), d.shape[0], out.ctypes.data_as(_dp)))
+    return out
+
+
+class SignedDistance:
+    """quest::SignedDistance<3, CUDA_EXEC> on the GB300 (quest/SignedDistance.hpp:147-605).
+
+    ``vertices`` (V, 3) and ``cells`` (C, 3 or 4) describe an unstructured
+    single-shape surface mesh (triangles or quads)."""
+
+    def __init__(self, vertices, cells, is_watertight: bool = True, compute_sign: bool = True,
+                 precision: int = PRECISION_FP64, sort_queries: bool = True):
+        self._lib = load()
+        v = np.ascontiguousarray(vertices, dtype=np.float64).reshape(-1, 3) if not _is_torch(vertices) \
+            else vertices.detach().to("cpu").double().reshape(-1, 3).numpy()
+        c = np.ascontiguousarray(cells, dtype=np.int32) if not _is_torch(cells) \
+            else cells.detach().to("cpu").int().numpy()
+        npc = c.shape[1] if c.ndim == 2 else 3
+        x, y, z = (np.ascontiguousarray(v[:, k]) for k in range(3))
+        self._opts = SdfOpts()
+        _check(self._lib.gsq_sdf_opts_init(C.byref(self._opts)))
+        self._opts.precision = precision
+        self._opts.sort_queries = int(sort_queries)
+        h = _vp()
+        _check(self._lib.gsq_sdf_create(C.byref(h), C.c_void_p(x.ctypes.data), C.c_void_p(y.ctypes.data),
+                                        C.c_void_p(z.ctypes.data), v.shape[0], C.c_void_p(c.ctypes.data),
+                                        c.size // npc, npc, int(is_watertight), int(compute_sign),
+                                        C.byref(self._opts), _stream()))
+        self._h = h
+
+    def __del__(self):
+        if getattr(self, "_h", None):
+            self._lib.gsq_sdf_destroy(self._h)
+            self._h = None
+
+    def set_precision(self, precision: int):
+        self._opts.precision = precision
+        _check(self._lib.gsq_sdf_set_opts(self._h, C.byref(self._opts)))
+
+    def set_sort_queries(self, on: bool):
+        self._opts.sort_queries = int(on)
+        _check(self._lib.gsq_sdf_set_opts(self._h, C.byref(self._opts)))
+
+    def compute_distances(self, points, closest: bool = False, normals: bool = False):
+        """Signed distances of (m, 3) points; optional closest points and unit normals."""
+        p = _Arr(points, np.float64, 3)
+        m = p.n
+        out = p.empty(m, np.float64)
+        cp = p.empty((m, 3), np.float64) if closest else None
+        nr = p.empty((m, 3), np.float64) if normals else None
+        base = p.ptr
+        _check(self._lib.gsq_sdf_eval(self._h, C.c_void_p(base), C.c_void_p(base + 8), C.c_void_p(base + 16), 3, m,
+                                      C.c_void_p(_ptr(out)), C.c_void_p(_ptr(cp)) if cp is not None else None,
+                                      C.c_void_p(_ptr(nr)) if nr is not None else None, _stream()))
+        if closest or normals:
+            return out, cp, nr
+        return out
+
+    def compute_distances_soa(self, x, y, z, out):
+        """signed_distance_evaluate(x, y, z, n, phi) form: three coordinate arrays."""
+        xs, ys, zs = (_Arr(a, np.float64) for a in (x, y, z))
+        _check(self._lib.gsq_sdf_eval(self._h, C.c_void_p(xs.ptr), C.c_void_p(ys.ptr), C.c_void_p(zs.ptr), 1,
+                                      xs.n, C.c_void_p(_ptr(out)), None, None, _stream()))
+        return out
+
+    def compute_distance(self, x: float, y: float, z: float) -> float:
+        return float(self.compute_distances(np.array([[x, y, z]]))[0])
+
+    def get_mesh_bounds(self):
+        lo, hi = np.empty(3), np.empty(3)
+        _check(self._lib.gsq_sdf_mesh_bounds(self._h, lo.ctypes.data_as(_dp), hi.ctypes.data_as(_dp)))
+        return lo, hi
+
+    def get_bvh_tree(self) -> BVH:
+        b = _vp()
+        _check(self._lib.gsq_sdf_get_bvh(self._h, C.byref(b)))
+        return BVH(_handle=b)
+
+    def last_eval_ms(self) -> float:
+        v = C.c_float()
+        _check(self._lib.gsq_sdf_last_eval_ms(self._h, C.byref(v)))
+        return v.value

@@ -1,0 +1,1033 @@
+// Linear BVH build and candidate queries on the GPU (spin::BVH replacement).
+//
+// Build pipeline (replaces build_radix_tree + emit_bvh_parents,
+// spin/internal/linear_bvh/build_radix_tree.hpp:579-611 and
+// spin/policy/LinearBVH.hpp:191-269):
+//   k_leaf_bounds   scale each box about its midpoint (transform_boxes,
+//                   BR:85-99) and fold the global bounds (reduce, BR:102-143)
+//   k_bounds_final  combine the per-block folds
+//   k_morton        30-bit Morton code of each scaled box centroid (get_mcodes,
+//                   BR:146-176)
+//   radix sort      stable (key, index) sort (sort_mcodes, BR:225-260)
+//   k_karras        Karras 2012 hierarchy, identical tie-breaking (build_tree,
+//                   BR:265-384)
+//   k_refit         bottom-up boxes with one atomic per node; the second
+//                   arrival continues (propagate_aabbs, BR:505-576), writing each
+//                   box straight into its parent's 128-byte node record (the
+//                   emit step fused in).  No thread ever waits on another.
+// Queries (replace findCandidatesImpl, LinearBVH.hpp:271-402): one thread per
+// query runs the reference traversal state machine (bvh_traverse.hpp:66-154);
+// pass 1 keeps up to CAP candidates per query in scratch and counts all of
+// them, a scan gives the CSR offsets, and pass 2 copies, re-traversing only
+// the queries with more than CAP candidates.
+#include "gsq_internal.cuh"
+
+#include <algorithm>
+#include <climits>
+#include <cstdlib>
+#include <cstring>
+#include <vector>
+
+using namespace gsq;
+
+namespace gsq
+{
+namespace
+{
+constexpr int BUILD_THREADS = 256;
+
+// (value, index) pairs folded "leftmost wins on ties", which reproduces the
+// strict-comparison updates of BoundingBox::addPoint applied in index order.
+struct ArgV
+{
+  double v;
+  int i;
+};
+__device__ __forceinline__ void take_min(ArgV& a, const ArgV& b)
+{
+  if(b.i != INT_MAX && (a.i == INT_MAX || b.v < a.v || (b.v == a.v && b.i < a.i))) a = b;
+}
+__device__ __forceinline__ void take_max(ArgV& a, const ArgV& b)
+{
+  if(b.i != INT_MAX && (a.i == INT_MAX || b.v > a.v || (b.v == a.v && b.i < a.i))) a = b;
+}
+__device__ __forceinline__ ArgV shfl_argv(const ArgV& a, int src)
+{
+  return ArgV {__shfl_sync(0xFFFFFFFFu, a.v, src), __shfl_sync(0xFFFFFFFFu, a.i, src)};
+}
+
+struct Fold
+{
+  ArgV lo[3], hi[3];
+  int first_valid;
+};
+
+__device__ __forceinline__ void fold_init(Fold& f)
+{
+  for(int d = 0; d < 3; ++d)
+  {
+    f.lo[d] = ArgV {0.0, INT_MAX};
+    f.hi[d] = ArgV {0.0, INT_MAX};
+  }
+  f.first_valid = INT_MAX;
+}
+
+__device__ __forceinline__ void fold_merge(Fold& a, const Fold& b)
+{
+  for(int d = 0; d < 3; ++d)
+  {
+    take_min(a.lo[d], b.lo[d]);
+    take_max(a.hi[d], b.hi[d]);
+  }
+  a.first_valid = min(a.first_valid, b.first_valid);
+}
+
+__device__ __forceinline__ void fold_warp(Fold& f)
+{
+  for(int off = 16; off > 0; off >>= 1)
+  {
+    Fold o;
+    for(int d = 0; d < 3; ++d)
+    {
+      o.lo[d] = shfl_argv(f.lo[d], (threadIdx.x & 31) + off < 32 ? (threadIdx.x & 31) + off : (threadIdx.x & 31));
+      o.hi[d] = shfl_argv(f.hi[d], (threadIdx.x & 31) + off < 32 ? (threadIdx.x & 31) + off : (threadIdx.x & 31));
+    }
+    o.first_valid = __shfl_sync(0xFFFFFFFFu, f.first_valid,
+                                (threadIdx.x & 31) + off < 32 ? (threadIdx.x & 31) + off : (threadIdx.x & 31));
+    fold_merge(f, o);
+  }
+}
+
+// Scaled leaf boxes + per-block folds of the bounds.
+//   BoundingBox::scale (BoundingBox.hpp:548-561): mid = 0.5*(lo+hi),
+//   r = (s*0.5)*(hi-lo), lo' = mid - r, hi' = mid + r, then checkAndFixBounds.
+//   reduce, SEQ branch (BR:134-141): addBox fold from an invalid box, i.e. the
+//   per-axis leftmost min of lo and leftmost max of "lo if lo == hi else hi"
+//   over valid boxes, with the first valid box contributing its own hi.
+__global__ void __launch_bounds__(BUILD_THREADS) k_leaf_bounds(const double* __restrict__ in,
+                                                                 int n,
+                                                                 double scale,
+                                                                 double* __restrict__ leaf,
+                                                                 Fold* __restrict__ partials)
+{
+  Fold f;
+  fold_init(f);
+  const double half = scale * 0.5;
+  for(int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+  {
+    double lo[3], hi[3];
+    for(int d = 0; d < 3; ++d)
+    {
+      lo[d] = in[6 * (size_t)i + d];
+      hi[d] = in[6 * (size_t)i + 3 + d];
+    }
+    const bool valid = box_valid(lo, hi);
+    if(valid)
+    {
+      for(int d = 0; d < 3; ++d)
+      {
+        const double mid = 0.5 * (lo[d] + hi[d]);
+        const double r = (hi[d] - lo[d]) * half;
+        lo[d] = mid - r;
+        hi[d] = mid + r;
+      }
+      for(int d = 0; d < 3; ++d)
+        if(lo[d] > hi[d])
+        {
+          const double t = lo[d];
+          lo[d] = hi[d];
+          hi[d] = t;
+        }
+      for(int d = 0; d < 3; ++d)
+      {
+        take_min(f.lo[d], ArgV {lo[d], i});
+        take_max(f.hi[d], ArgV {(lo[d] == hi[d]) ? lo[d] : hi[d], i});
+      }
+      f.first_valid = min(f.first_valid, i);
+    }
+    for(int d = 0; d < 3; ++d)
+    {
+      leaf[6 * (size_t)i + d] = lo[d];
+      leaf[6 * (size_t)i + 3 + d] = hi[d];
+    }
+  }
+  fold_warp(f);
+  __shared__ Fold s_f[BUILD_THREADS / 32];
+  if((threadIdx.x & 31) == 0) s_f[threadIdx.x >> 5] = f;
+  __syncthreads();
+  if(threadIdx.x == 0)
+  {
+    Fold a = s_f[0];
+    for(int w = 1; w < BUILD_THREADS / 32; ++w) fold_merge(a, s_f[w]);
+    partials[blockIdx.x] = a;
+  }
+}
+
+// params: bounds lo[3] hi[3], then Morton min[3], inv_extent[3].
+__global__ void k_bounds_final(const Fold* __restrict__ partials, int nb, const double* __restrict__ leaf, int n,
+                               double* __restrict__ params)
+{
+  if(threadIdx.x != 0 || blockIdx.x != 0) return;
+  Fold a = partials[0];
+  for(int b = 1; b < nb; ++b) fold_merge(a, partials[b]);
+  double lo[3], hi[3];
+  if(a.first_valid == INT_MAX)
+  {
+    // no valid box: the fold ends as a copy of the last box
+    for(int d = 0; d < 3; ++d)
+    {
+      lo[d] = leaf[6 * (size_t)(n - 1) + d];
+      hi[d] = leaf[6 * (size_t)(n - 1) + 3 + d];
+    }
+  }
+  else
+  {
+    for(int d = 0; d < 3; ++d)
+    {
+      lo[d] = a.lo[d].v;
+      hi[d] = (a.hi[d].i == a.first_valid) ? leaf[6 * (size_t)a.first_valid + 3 + d] : a.hi[d].v;
+    }
+  }
+  for(int d = 0; d < 3; ++d)
+  {
+    params[d] = lo[d];
+    params[3 + d] = hi[d];
+    // get_mcodes (BR:154-163): inv_extent = isNearlyEqual(extent, 0) ? 0 : 1/extent
+    const double ext = hi[d] - lo[d];
+    params[6 + d] = lo[d];
+    params[9 + d] = (fabs(ext - 0.0) <= 1.0e-8) ? 0.0 : 1.0 / ext;
+  }
+}
+
+// 10-bit spread for a 3D Morton interleave (Ericson's magic numbers; the
+// reference's Mortonizer<int32,int32,3>::expandBits, spin/MortonIndex.hpp:151-159).
+__device__ __forceinline__ uint32_t spread10(uint32_t x)
+{
+  x = (x | (x << 16)) & 0xFF0000FFu;
+  x = (x | (x << 8)) & 0x0F00F00Fu;
+  x = (x | (x << 4)) & 0xC30C30C3u;
+  x = (x | (x << 2)) & 0x49249249u;
+  return x;
+}
+
+// morton32_encode (BR:48-65) of the normalised centroid (BR:165-175).
+__global__ void __launch_bounds__(BUILD_THREADS) k_morton(const double* __restrict__ leaf,
+                                                            int n,
+                                                            const double* __restrict__ params,
+                                                            uint32_t* __restrict__ codes)
+{
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if(i >= n) return;
+  uint32_t q[3];
+  for(int d = 0; d < 3; ++d)
+  {
+    const double mid = 0.5 * (leaf[6 * (size_t)i + d] + leaf[6 * (size_t)i + 3 + d]);
+    const double c = (mid - params[6 + d]) * params[9 + d];
+    q[d] = (uint32_t)(int)fmin(fmax(c * 1024.0, 0.0), 1023.0);
+  }
+  codes[i] = spread10(q[0]) | (spread10(q[1]) << 1) | (spread10(q[2]) << 2);
+}
+
+// delta (BR:265-287)
+__device__ __forceinline__ int delta(int a, int b, int inner, const uint32_t* __restrict__ codes)
+{
+  const bool oor = (b < 0 || b > inner);
+  const int bb = oor ? 0 : b;
+  uint32_t x = __ldg(codes + a) ^ __ldg(codes + bb);
+  const bool tie = (x == 0);
+  if(tie) x = (uint32_t)a ^ (uint32_t)bb;
+  int c = __clz(x);
+  if(tie) c += 32;
+  return oor ? -1 : c;
+}
+
+// build_tree (BR:290-384); also writes the child links of each node record.
+__global__ void __launch_bounds__(BUILD_THREADS) k_karras(const uint32_t* __restrict__ codes,
+                                                            int n,
+                                                            int* __restrict__ lchild,
+                                                            int* __restrict__ rchild,
+                                                            int* __restrict__ parent,
+                                                            NodeRec64* __restrict__ nodes)
+{
+  const int inner = n - 1;
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if(i >= inner) return;
+  const int dir = (delta(i, i + 1, inner, codes) - delta(i, i - 1, inner, codes)) < 0 ? -1 : 1;
+  const int dmin = delta(i, i - dir, inner, codes);
+  int lmax = 2;
+  while(delta(i, i + lmax * dir, inner, codes) > dmin) lmax *= 2;
+  int l = 0;
+  for(int s = lmax / 2; s >= 1; s /= 2)
+    if(delta(i, i + (l + s) * dir, inner, codes) > dmin) l += s;
+  const int j = i + l * dir;
+  const int dnode = delta(i, j, inner, codes);
+  int s = 0;
+  double div = 2.0;
+  for(int st = (int)ceil(double(float(l)) / div);; div *= 2.0, st = (int)ceil(double(float(l)) / div))
+  {
+    if(delta(i, i + (s + st) * dir, inner, codes) > dnode) s += st;
+    if(st == 1) break;
+  }
+  const int split = i + s * dir + min(dir, 0);
+  int lc, rc;
+  if(min(i, j) == split)
+  {
+    parent[split + inner] = i;
+    lc = split + inner;
+  }
+  else
+  {
+    parent[split] = i;
+    lc = split;
+  }
+  if(max(i, j) == split + 1)
+  {
+    parent[split + inner + 1] = i;
+    rc = split + inner + 1;
+  }
+  else
+  {
+    parent[split + 1] = i;
+    rc = split + 1;
+  }
+  lchild[i] = lc;
+  rchild[i] = rc;
+  nodes[i].child[0] = (lc >= inner) ? -(lc - inner + 1) : lc;
+  nodes[i].child[1] = (rc >= inner) ? -(rc - inner + 1) : rc;
+  if(i == 0) parent[0] = -1;
+}
+
+// BoundingBox::addBox (BoundingBox.hpp:487-505) into acc.
+__device__ __forceinline__ void add_box(double* alo, double* ahi, const double* lo, const double* hi)
+{
+  if(box_valid(alo, ahi))
+  {
+    if(box_valid(lo, hi))
+    {
+      for(int d = 0; d < 3; ++d)
+      {
+        if(lo[d] < alo[d]) alo[d] = lo[d];
+        if(lo[d] > ahi[d]) ahi[d] = lo[d];
+      }
+      for(int d = 0; d < 3; ++d)
+      {
+        if(hi[d] < alo[d]) alo[d] = hi[d];
+        if(hi[d] > ahi[d]) ahi[d] = hi[d];
+      }
+    }
+  }
+  else
+    for(int d = 0; d < 3; ++d)
+    {
+      alo[d] = lo[d];
+      ahi[d] = hi[d];
+    }
+}
+
+// propagate_aabbs (BR:505-576) fused with emit_bvh_parents (LB:225-264).
+// One thread per sorted leaf.  A thread stores its box into its parent's
+// record, fences, and bumps the parent's counter; the first arrival exits and
+// the second combines the two child boxes as the reference's SEQ order does
+// (box(node) = addBox(box(right), box(left))) and moves up.
+__global__ void __launch_bounds__(BUILD_THREADS) k_refit(const double* __restrict__ leaf,
+                                                           const int* __restrict__ perm,
+                                                           int n,
+                                                           const int* __restrict__ lchild,
+                                                           const int* __restrict__ parent,
+                                                           int* __restrict__ counters,
+                                                           NodeRec64* nodes,
+                                                           double* __restrict__ root_box)
+{
+  const int inner = n - 1;
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if(k >= n) return;
+  const int id = perm[k];
+  double lo[3], hi[3];
+  for(int d = 0; d < 3; ++d)
+  {
+    lo[d] = leaf[6 * (size_t)id + d];
+    hi[d] = leaf[6 * (size_t)id + 3 + d];
+  }
+  int last = inner + k;
+  int node = parent[inner + k];
+  while(true)
+  {
+    const int side = (lchild[node] == last) ? 0 : 1;
+    double* dst = nodes[node].b + 6 * side;
+    for(int d = 0; d < 3; ++d)
+    {
+      dst[d] = lo[d];
+      dst[3 + d] = hi[d];
+    }
+    __threadfence();
+    if(atomicAdd(&counters[node], 1) == 0) return;
+    __threadfence();
+    const double* b = nodes[node].b;
+    double llo[3], lhi[3];
+    for(int d = 0; d < 3; ++d)
+    {
+      lo[d] = __ldcg(b + 6 + d);   // right child box
+      hi[d] = __ldcg(b + 9 + d);
+      llo[d] = __ldcg(b + d);      // left child box
+      lhi[d] = __ldcg(b + 3 + d);
+    }
+    add_box(lo, hi, llo, lhi);
+    last = node;
+    node = parent[node];
+    if(node == -1)
+    {
+      for(int d = 0; d < 3; ++d)
+      {
+        root_box[d] = lo[d];
+        root_box[3 + d] = hi[d];
+      }
+      return;
+    }
+  }
+}
+
+// ---- traversal --------------------------------------------------------------
+// bvh_traverse (bvh_traverse.hpp:66-154) with the generic traverser's
+// no-preference order (LB:92-103).  pred(lo, hi) tests one child box; leaf
+// receives the sorted leaf position.  Returns false on stack overflow.
+template <class Pred, class Leaf>
+__device__ __forceinline__ bool traverse_nopref(const NodeRec64* __restrict__ nodes, Pred& pred, Leaf& leaf)
+{
+  int todo[STACK_SIZE];
+  int sp = 0;
+  todo[0] = BARRIER;
+  int found = 0, cur = 0;
+  while(cur != BARRIER)
+  {
+    while(cur >= 0)
+    {
+      const double2* r = reinterpret_cast<const double2*>(nodes + cur);
+      double b[12];
+#pragma unroll
+      for(int k = 0; k < 6; ++k)
+      {
+        const double2 v = __ldg(r + k);
+        b[2 * k] = v.x;
+        b[2 * k + 1] = v.y;
+      }
+      const int2 ch = __ldg(reinterpret_cast<const int2*>(nodes[cur].child));
+      const bool inL = box_valid(b, b + 3) ? pred(b, b + 3) : false;
+      const bool inR = box_valid(b + 6, b + 9) ? pred(b + 6, b + 9) : false;
+      if(!inL && !inR)
+        cur = (sp >= 0) ? todo[sp--] : BARRIER;
+      else
+      {
+        cur = inL ? ch.x : ch.y;
+        if(inL && inR)
+        {
+          if(sp + 1 >= STACK_SIZE) return false;
+          todo[++sp] = ch.y;
+        }
+      }
+      if(cur < 0 && !(found < 0))
+      {
+        found = cur;
+        if(cur != BARRIER) cur = (sp >= 0) ? todo[sp--] : BARRIER;
+      }
+    }
+    while(found < 0 && found != BARRIER)
+    {
+      leaf(-found - 1);
+      found = cur;
+      if(cur < 0 && cur != BARRIER) cur = (sp >= 0) ? todo[sp--] : BARRIER;
+    }
+    found = 0;
+  }
+  return true;
+}
+
+// Query primitives.  Boxes: BoundingBox::intersectsWith with
+// intersect_bbox_bbox (BoundingBox.hpp:432-447, intersect_bounding_box_impl.hpp:35-41).
+struct BoxQuery
+{
+  double lo[3], hi[3];
+  __device__ bool operator()(const double* blo, const double* bhi) const
+  {
+    for(int d = 0; d < 3; ++d)
+      if(!(hi[d] >= blo[d] && lo[d] <= bhi[d])) return false;
+    return true;
+  }
+};
+// Points: BoundingBox::contains(Point) (BoundingBox.hpp:388-401).
+struct PointQuery
+{
+  double p[3];
+  __device__ bool operator()(const double* blo, const double* bhi) const
+  {
+    for(int d = 0; d < 3; ++d)
+      if(p[d] < blo[d] || p[d] > bhi[d]) return false;
+    return true;
+  }
+};
+// Rays: intersect_ray(Ray, BoundingBox, Point&, EPS) and
+// intersect_ray_bbox_test (intersect_ray_impl.hpp:151-186, 321-351).
+struct RayQuery
+{
+  double o[3], n[3], eps;
+  __device__ bool operator()(const double* blo, const double* bhi) const
+  {
+    double tmin = DBL_MIN, tmax = DBL_MAX;
+    for(int d = 0; d < 3; ++d)
+    {
+      bool ok;
+      if(fabs(n[d] - 0.0) <= eps)
+        ok = !((o[d] < blo[d]) || (o[d] > bhi[d]));
+      else
+      {
+        const double inv = 1.0 / n[d];
+        double t1 = (blo[d] - o[d]) * inv;
+        double t2 = (bhi[d] - o[d]) * inv;
+        if(t1 > t2)
+        {
+          const double t = t1;
+          t1 = t2;
+          t2 = t;
+        }
+        tmin = (t1 < tmin) ? tmin : t1;
+        tmax = (t2 < tmax) ? t2 : tmax;
+        ok = !(tmin > tmax);
+      }
+      if(!ok) return false;
+    }
+    return true;
+  }
+};
+
+enum QueryKind
+{
+  Q_BOXES = 0,
+  Q_POINTS = 1,
+  Q_RAYS = 2
+};
+
+struct QueryArgs
+{
+  const double* a;  // boxes (m x 6), points (m x 3) or ray origins (m x 3)
+  const double* b;  // ray directions (m x 3)
+  double eps;
+};
+
+template <int KIND>
+__device__ __forceinline__ auto make_query(const QueryArgs& q, int i)
+{
+  if constexpr(KIND == Q_BOXES)
+  {
+    BoxQuery bq;
+    for(int d = 0; d < 3; ++d)
+    {
+      bq.lo[d] = q.a[6 * (size_t)i + d];
+      bq.hi[d] = q.a[6 * (size_t)i + 3 + d];
+    }
+    return bq;
+  }
+  else if constexpr(KIND == Q_POINTS)
+  {
+    PointQuery pq;
+    for(int d = 0; d < 3; ++d) pq.p[d] = q.a[3 * (size_t)i + d];
+    return pq;
+  }
+  else
+  {
+    RayQuery rq;
+    for(int d = 0; d < 3; ++d)
+    {
+      rq.o[d] = q.a[3 * (size_t)i + d];
+      rq.n[d] = q.b[3 * (size_t)i + d];
+    }
+    rq.eps = q.eps;
+    return rq;
+  }
+}
+
+constexpr int FIND_THREADS = 128;
+constexpr int FIND_CAP = 8;  // candidates kept per query by pass 1
+
+template <int KIND>
+__global__ void __launch_bounds__(FIND_THREADS) k_find_pass1(const NodeRec64* __restrict__ nodes,
+                                                               const int* __restrict__ perm,
+                                                               QueryArgs qa,
+                                                               int m,
+                                                               int* __restrict__ counts,
+                                                               int* __restrict__ keep,
+                                                               int* err)
+{
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if(i >= m) return;
+  auto pred = make_query<KIND>(qa, i);
+  int c = 0;
+  int* mine = keep + (size_t)i * FIND_CAP;
+  auto leaf = [&](int leafpos) {
+    if(c < FIND_CAP) mine[c] = __ldg(perm + leafpos);
+    ++c;
+  };
+  if(!traverse_nopref(nodes, pred, leaf)) atomicOr(err, DEVERR_STACK);
+  counts[i] = c;
+}
+
+template <int KIND>
+__global__ void __launch_bounds__(FIND_THREADS) k_find_pass2(const NodeRec64* __restrict__ nodes,
+                                                               const int* __restrict__ perm,
+                                                               QueryArgs qa,
+                                                               int m,
+                                                               const int* __restrict__ counts,
+                                                               const int* __restrict__ offsets,
+                                                               const int* __restrict__ keep,
+                                                               int* __restrict__ cand)
+{
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if(i >= m) return;
+  const int c = counts[i];
+  int* out = cand + offsets[i];
+  if(c <= FIND_CAP)
+  {
+    for(int k = 0; k < c; ++k) out[k] = keep[(size_t)i * FIND_CAP + k];
+    return;
+  }
+  auto pred = make_query<KIND>(qa, i);
+  int w = 0;
+  auto leaf = [&](int leafpos) {
+    if(w < c) out[w] = __ldg(perm + leafpos);
+    ++w;
+  };
+  traverse_nopref(nodes, pred, leaf);
+}
+
+inline int grid_for(long long n, int threads) { return (int)std::max<long long>(1, (n + threads - 1) / threads); }
+
+// Mesh box: BoundingBox::addPoint over the nodes in order from an invalid box
+// (quest/SignedDistance.hpp:483-486) = per axis leftmost min and leftmost max.
+__global__ void __launch_bounds__(BUILD_THREADS) k_node_fold(const double* __restrict__ x,
+                                                               const double* __restrict__ y,
+                                                               const double* __restrict__ z,
+                                                               int nv,
+                                                               Fold* __restrict__ partials)
+{
+  Fold f;
+  fold_init(f);
+  for(int i = blockIdx.x * blockDim.x + threadIdx.x; i < nv; i += gridDim.x * blockDim.x)
+  {
+    const double p[3] = {x[i], y[i], z[i]};
+    for(int d = 0; d < 3; ++d)
+    {
+      take_min(f.lo[d], ArgV {p[d], i});
+      take_max(f.hi[d], ArgV {p[d], i});
+    }
+  }
+  fold_warp(f);
+  __shared__ Fold s_f[BUILD_THREADS / 32];
+  if((threadIdx.x & 31) == 0) s_f[threadIdx.x >> 5] = f;
+  __syncthreads();
+  if(threadIdx.x == 0)
+  {
+    Fold a = s_f[0];
+    for(int w = 1; w < BUILD_THREADS / 32; ++w) fold_merge(a, s_f[w]);
+    partials[blockIdx.x] = a;
+  }
+}
+
+__global__ void k_node_final(const Fold* __restrict__ partials, int nb, double* __restrict__ out)
+{
+  if(threadIdx.x != 0 || blockIdx.x != 0) return;
+  Fold a = partials[0];
+  for(int b = 1; b < nb; ++b) fold_merge(a, partials[b]);
+  for(int d = 0; d < 3; ++d)
+  {
+    out[d] = (a.lo[d].i == INT_MAX) ? DBL_MAX : a.lo[d].v;
+    out[3 + d] = (a.hi[d].i == INT_MAX) ? -DBL_MAX : a.hi[d].v;
+  }
+}
+
+}  // namespace
+
+int node_bounds(const double* x, const double* y, const double* z, int nv, double* out6, cudaStream_t s)
+{
+  const int nb = std::min(grid_for(std::max(nv, 1), BUILD_THREADS), 4 * 152);
+  Scratch work;
+  GSQ_CUDA_TRY(work.alloc(sizeof(Fold) * nb + 256, s));
+  Fold* folds = work.as<Fold>();
+  double* d_out = reinterpret_cast<double*>(reinterpret_cast<char*>(folds) + ((sizeof(Fold) * nb + 15) & ~size_t(15)));
+  k_node_fold<<<nb, BUILD_THREADS, 0, s>>>(x, y, z, nv, folds);
+  k_node_final<<<1, 32, 0, s>>>(folds, nb, d_out);
+  count_launch(2);
+  GSQ_CUDA_TRY(cudaGetLastError());
+  GSQ_CUDA_TRY(cudaMemcpyAsync(out6, d_out, sizeof(double) * 6, cudaMemcpyDeviceToHost, s));
+  GSQ_CUDA_TRY(cudaStreamSynchronize(s));
+  return GSQ_OK;
+}
+
+void BvhDev::release()
+{
+  if(block) cudaFree(block);
+  block = nullptr;
+  block_bytes = 0;
+  nodes = nullptr;
+  perm = nullptr;
+  codes = nullptr;
+  lchild = rchild = nullptr;
+  n = 0;
+}
+
+int bvh_build(BvhDev& B, const double* d_boxes, int n, double scale, cudaStream_t s, int* d_err)
+{
+  if(n < 0) return fail(GSQ_ERR_INVALID, "number of boxes must be >= 0");
+  // BVH::initialize (spin/BVH.hpp:436-463): 0 or 1 boxes -> 2, second invalid.
+  Scratch pad;
+  if(n <= 1)
+  {
+    double h[12];
+    for(int d = 0; d < 3; ++d)
+    {
+      h[d] = h[6 + d] = DBL_MAX;
+      h[3 + d] = h[9 + d] = -DBL_MAX;
+    }
+    GSQ_CUDA_TRY(pad.alloc(sizeof(h), s));
+    GSQ_CUDA_TRY(cudaMemcpyAsync(pad.p, h, sizeof(h), cudaMemcpyHostToDevice, s));
+    if(n == 1) GSQ_CUDA_TRY(cudaMemcpyAsync(pad.p, d_boxes, 6 * sizeof(double), cudaMemcpyDeviceToDevice, s));
+    d_boxes = pad.as<double>();
+    n = 2;
+  }
+  const int inner = n - 1;
+
+  // Persistent arrays in one allocation.
+  auto align = [](size_t x) { return (x + 255) & ~size_t(255); };
+  const size_t sz_nodes = align(sizeof(NodeRec64) * inner);
+  const size_t sz_perm = align(sizeof(int) * n);
+  const size_t sz_codes = align(sizeof(uint32_t) * n);
+  const size_t sz_child = align(sizeof(int) * inner);
+  const size_t total = sz_nodes + sz_perm + sz_codes + 2 * sz_child;
+  if(total > B.block_bytes)
+  {
+    B.release();
+    GSQ_CUDA_TRY(cudaMalloc(&B.block, total));
+    B.block_bytes = total;
+  }
+  char* base = static_cast<char*>(B.block);
+  B.n = n;
+  B.nodes = reinterpret_cast<NodeRec64*>(base);
+  B.perm = reinterpret_cast<int*>(base + sz_nodes);
+  B.codes = reinterpret_cast<uint32_t*>(base + sz_nodes + sz_perm);
+  B.lchild = reinterpret_cast<int*>(base + sz_nodes + sz_perm + sz_codes);
+  B.rchild = reinterpret_cast<int*>(base + sz_nodes + sz_perm + sz_codes + sz_child);
+
+  // Scratch: leaf boxes, params, codes/vals ping-pong, parents, counters, folds.
+  const int fold_blocks = std::min(grid_for(n, BUILD_THREADS), 4 * 152);
+  const size_t sz_leaf = align(sizeof(double) * 6 * (size_t)n);
+  const size_t sz_params = align(sizeof(double) * 18);
+  const size_t sz_u32 = align(sizeof(uint32_t) * n);
+  const size_t sz_par = align(sizeof(int) * (2 * (size_t)n - 1));
+  const size_t sz_cnt = align(sizeof(int) * inner);
+  const size_t sz_fold = align(sizeof(Fold) * fold_blocks);
+  Scratch work;
+  GSQ_CUDA_TRY(work.alloc(sz_leaf + sz_params + 4 * sz_u32 + sz_par + sz_cnt + sz_fold, s));
+  char* w = work.as<char>();
+  double* leaf = reinterpret_cast<double*>(w);
+  w += sz_leaf;
+  double* params = reinterpret_cast<double*>(w);
+  w += sz_params;
+  uint32_t* keys[2] = {reinterpret_cast<uint32_t*>(w), reinterpret_cast<uint32_t*>(w + sz_u32)};
+  w += 2 * sz_u32;
+  int* vals[2] = {reinterpret_cast<int*>(w), reinterpret_cast<int*>(w + sz_u32)};
+  w += 2 * sz_u32;
+  int* parent = reinterpret_cast<int*>(w);
+  w += sz_par;
+  int* counters = reinterpret_cast<int*>(w);
+  w += sz_cnt;
+  Fold* folds = reinterpret_cast<Fold*>(w);
+
+  k_leaf_bounds<<<fold_blocks, BUILD_THREADS, 0, s>>>(d_boxes, n, scale, leaf, folds);
+  k_bounds_final<<<1, 32, 0, s>>>(folds, fold_blocks, leaf, n, params);
+  k_morton<<<grid_for(n, BUILD_THREADS), BUILD_THREADS, 0, s>>>(leaf, n, params, keys[0]);
+  const int which = radix_sort_pairs(keys, vals, n, 30, true, s, d_err);
+  if(which < 0) return which;
+  GSQ_CUDA_TRY(cudaMemcpyAsync(B.codes, keys[which], sizeof(uint32_t) * n, cudaMemcpyDeviceToDevice, s));
+  GSQ_CUDA_TRY(cudaMemcpyAsync(B.perm, vals[which], sizeof(int) * n, cudaMemcpyDeviceToDevice, s));
+  k_karras<<<grid_for(inner, BUILD_THREADS), BUILD_THREADS, 0, s>>>(B.codes, n, B.lchild, B.rchild, parent, B.nodes);
+  GSQ_CUDA_TRY(cudaMemsetAsync(counters, 0, sizeof(int) * inner, s));
+  k_refit<<<grid_for(n, BUILD_THREADS), BUILD_THREADS, 0, s>>>(leaf, B.perm, n, B.lchild, parent, counters, B.nodes,
+                                                               params + 12);
+  count_launch(5);
+  GSQ_CUDA_TRY(cudaGetLastError());
+  GSQ_CUDA_TRY(cudaMemcpyAsync(B.bounds, params, sizeof(double) * 6, cudaMemcpyDeviceToHost, s));
+  GSQ_CUDA_TRY(cudaStreamSynchronize(s));
+  return check_device_error(d_err, s, "bvh build");
+}
+
+}  // namespace gsq
+
+// =============================================================================
+// C ABI: spin::BVH
+// =============================================================================
+struct gsq_bvh
+{
+  int device = 0;
+  double scale = gsq::DEFAULT_SCALE;
+  double tol = DBL_EPSILON;
+  gsq::BvhDev dev;
+  bool built = false;
+  float build_ms = 0.f;
+  int* d_err = nullptr;
+};
+
+namespace
+{
+int check_bvh(const gsq_bvh* h)
+{
+  if(!h) return fail(GSQ_ERR_INVALID, "null bvh handle");
+  if(!h->built) return fail(GSQ_ERR_STATE, "bvh has not been built");
+  return GSQ_OK;
+}
+
+template <int KIND>
+int find_impl(const gsq_bvh* h, const double* a, const double* b, int32_t m, int32_t* offsets, int32_t* counts,
+              int32_t** candidates, int64_t* total_out, void* stream)
+{
+  int rc = check_bvh(h);
+  if(rc) return rc;
+  if(m < 0 || !candidates || (m > 0 && (!a || !offsets || !counts || (KIND == Q_RAYS && !b))))
+    return fail(GSQ_ERR_INVALID, "invalid find arguments");
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  const bool dev_out = offsets ? is_device_ptr(offsets) : false;
+  *candidates = nullptr;
+  const int width = (KIND == Q_BOXES) ? 6 : 3;
+  InBuf qa_buf, qb_buf;
+  GSQ_CUDA_TRY(qa_buf.stage(a, sizeof(double) * width * (size_t)m, s));
+  if(KIND == Q_RAYS) GSQ_CUDA_TRY(qb_buf.stage(b, sizeof(double) * 3 * (size_t)m, s));
+  OutBuf off_buf, cnt_buf;
+  GSQ_CUDA_TRY(off_buf.prepare(offsets, sizeof(int) * (size_t)m, s));
+  GSQ_CUDA_TRY(cnt_buf.prepare(counts, sizeof(int) * (size_t)m, s));
+  Scratch keep, tot;
+  GSQ_CUDA_TRY(keep.alloc(sizeof(int) * FIND_CAP * (size_t)std::max(m, 1), s));
+  GSQ_CUDA_TRY(tot.alloc(sizeof(long long), s));
+  QueryArgs qa {static_cast<const double*>(qa_buf.dev), static_cast<const double*>(qb_buf.dev), h->tol};
+  int* d_cnt = static_cast<int*>(cnt_buf.dev);
+  int* d_off = static_cast<int*>(off_buf.dev);
+  if(m > 0)
+  {
+    count_launch();
+    k_find_pass1<KIND><<<grid_for(m, FIND_THREADS), FIND_THREADS, 0, s>>>(h->dev.nodes, h->dev.perm, qa, m, d_cnt,
+                                                                          keep.as<int>(), h->d_err);
+  }
+  rc = exclusive_scan(d_cnt, d_off, m, tot.as<long long>(), s);
+  if(rc) return rc;
+  long long total = 0;
+  GSQ_CUDA_TRY(cudaMemcpyAsync(&total, tot.p, sizeof(long long), cudaMemcpyDeviceToHost, s));
+  GSQ_CUDA_TRY(cudaStreamSynchronize(s));
+  rc = check_device_error(h->d_err, s, "find pass 1");
+  if(rc) return rc;
+  if(total > INT_MAX) return fail(GSQ_ERR_INVALID, "more than 2^31-1 candidates");
+  int* d_cand = nullptr;
+  GSQ_CUDA_TRY(cudaMalloc(&d_cand, sizeof(int) * (size_t)std::max<long long>(total, 1)));
+  if(m > 0)
+  {
+    count_launch();
+    k_find_pass2<KIND><<<grid_for(m, FIND_THREADS), FIND_THREADS, 0, s>>>(h->dev.nodes, h->dev.perm, qa, m, d_cnt,
+                                                                          d_off, keep.as<int>(), d_cand);
+  }
+  cudaError_t e = cudaGetLastError();
+  if(e == cudaSuccess) e = off_buf.flush(s);
+  if(e == cudaSuccess) e = cnt_buf.flush(s);
+  if(e == cudaSuccess && !dev_out)
+  {
+    int* host = static_cast<int*>(std::malloc(sizeof(int) * (size_t)std::max<long long>(total, 1)));
+    if(!host)
+      e = cudaErrorMemoryAllocation;
+    else
+    {
+      e = cudaMemcpyAsync(host, d_cand, sizeof(int) * (size_t)total, cudaMemcpyDeviceToHost, s);
+      if(e == cudaSuccess) e = cudaStreamSynchronize(s);
+      cudaFree(d_cand);
+      d_cand = nullptr;
+      *candidates = host;
+      if(e != cudaSuccess)
+      {
+        std::free(host);
+        *candidates = nullptr;
+      }
+    }
+  }
+  else
+    *candidates = d_cand;
+  if(e == cudaSuccess) e = cudaStreamSynchronize(s);
+  if(e != cudaSuccess)
+  {
+    if(d_cand) cudaFree(d_cand);
+    *candidates = nullptr;
+    return cuda_fail(e, "find pass 2");
+  }
+  if(total_out) *total_out = total;
+  return GSQ_OK;
+}
+}  // namespace
+
+extern "C" {
+
+int gsq_bvh_create(gsq_bvh** out)
+{
+  if(!out) return fail(GSQ_ERR_INVALID, "null output pointer");
+  auto* h = new(std::nothrow) gsq_bvh();
+  if(!h) return fail(GSQ_ERR_NOMEM, "handle allocation failed");
+  cudaError_t e = cudaGetDevice(&h->device);
+  if(e == cudaSuccess) e = cudaMalloc(&h->d_err, sizeof(int));
+  if(e == cudaSuccess) e = cudaMemset(h->d_err, 0, sizeof(int));
+  if(e != cudaSuccess)
+  {
+    delete h;
+    return cuda_fail(e, "gsq_bvh_create");
+  }
+  *out = h;
+  return GSQ_OK;
+}
+
+int gsq_bvh_destroy(gsq_bvh* h)
+{
+  if(!h) return GSQ_OK;
+  h->dev.release();
+  if(h->d_err) cudaFree(h->d_err);
+  delete h;
+  return GSQ_OK;
+}
+
+int gsq_bvh_set_scale_factor(gsq_bvh* h, double s)
+{
+  if(!h) return fail(GSQ_ERR_INVALID, "null bvh handle");
+  h->scale = s;
+  return GSQ_OK;
+}
+int gsq_bvh_get_scale_factor(const gsq_bvh* h, double* s)
+{
+  if(!h || !s) return fail(GSQ_ERR_INVALID, "null argument");
+  *s = h->scale;
+  return GSQ_OK;
+}
+int gsq_bvh_set_tolerance(gsq_bvh* h, double t)
+{
+  if(!h) return fail(GSQ_ERR_INVALID, "null bvh handle");
+  h->tol = t;
+  return GSQ_OK;
+}
+int gsq_bvh_get_tolerance(const gsq_bvh* h, double* t)
+{
+  if(!h || !t) return fail(GSQ_ERR_INVALID, "null argument");
+  *t = h->tol;
+  return GSQ_OK;
+}
+
+int gsq_bvh_build(gsq_bvh* h, const double* boxes, int32_t n, void* stream)
+{
+  if(!h) return fail(GSQ_ERR_INVALID, "null bvh handle");
+  if(n < 0 || (n > 0 && !boxes)) return fail(GSQ_ERR_INVALID, "invalid boxes");
+  if(n >= (1 << 30)) return fail(GSQ_ERR_INVALID, "at most 2^30-1 boxes");
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  h->built = false;
+  InBuf in;
+  GSQ_CUDA_TRY(in.stage(boxes, sizeof(double) * 6 * (size_t)n, s));
+  cudaEvent_t e0, e1;
+  GSQ_CUDA_TRY(cudaEventCreate(&e0));
+  GSQ_CUDA_TRY(cudaEventCreate(&e1));
+  cudaEventRecord(e0, s);
+  const int rc = bvh_build(h->dev, static_cast<const double*>(in.dev), n, h->scale, s, h->d_err);
+  cudaEventRecord(e1, s);
+  cudaEventSynchronize(e1);
+  cudaEventElapsedTime(&h->build_ms, e0, e1);
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  if(rc) return rc;
+  h->built = true;
+  return GSQ_OK;
+}
+
+int gsq_bvh_bounds(const gsq_bvh* h, double* lo, double* hi)
+{
+  int rc = check_bvh(h);
+  if(rc) return rc;
+  if(!lo || !hi) return fail(GSQ_ERR_INVALID, "null argument");
+  for(int d = 0; d < 3; ++d)
+  {
+    lo[d] = h->dev.bounds[d];
+    hi[d] = h->dev.bounds[3 + d];
+  }
+  return GSQ_OK;
+}
+
+int gsq_bvh_num_leaves(const gsq_bvh* h, int32_t* n)
+{
+  int rc = check_bvh(h);
+  if(rc) return rc;
+  if(!n) return fail(GSQ_ERR_INVALID, "null argument");
+  *n = h->dev.n;
+  return GSQ_OK;
+}
+
+int gsq_bvh_last_build_ms(const gsq_bvh* h, float* ms)
+{
+  if(!h || !ms) return fail(GSQ_ERR_INVALID, "null argument");
+  *ms = h->build_ms;
+  return GSQ_OK;
+}
+
+int gsq_bvh_find_boxes(const gsq_bvh* h, const double* q, int32_t m, int32_t* offsets, int32_t* counts,
+                       int32_t** candidates, int64_t* total, void* stream)
+{
+  return find_impl<Q_BOXES>(h, q, nullptr, m, offsets, counts, candidates, total, stream);
+}
+
+int gsq_bvh_find_points(const gsq_bvh* h, const double* p, int32_t m, int32_t* offsets, int32_t* counts,
+                        int32_t** candidates, int64_t* total, void* stream)
+{
+  return find_impl<Q_POINTS>(h, p, nullptr, m, offsets, counts, candidates, total, stream);
+}
+
+int gsq_bvh_find_rays(const gsq_bvh* h, const double* o, const double* d, int32_t m, int32_t* offsets,
+                      int32_t* counts, int32_t** candidates, int64_t* total, void* stream)
+{
+  return find_impl<Q_RAYS>(h, o, d, m, offsets, counts, candidates, total, stream);
+}
+
+int gsq_bvh_export(const gsq_bvh* h, double* node_boxes, int32_t* children, int32_t* leaf_ids, uint32_t* codes)
+{
+  int rc = check_bvh(h);
+  if(rc) return rc;
+  const int n = h->dev.n, inner = n - 1;
+  std::vector<NodeRec64> recs(inner);
+  GSQ_CUDA_TRY(cudaMemcpy(recs.data(), h->dev.nodes, sizeof(NodeRec64) * inner, cudaMemcpyDeviceToHost));
+  for(int i = 0; i < inner; ++i)
+  {
+    if(node_boxes) std::memcpy(node_boxes + 12 * (size_t)i, recs[i].b, sizeof(double) * 12);
+    if(children)
+      for(int k = 0; k < 2; ++k)
+      {
+        const int c = recs[i].child[k];
+        children[2 * i + k] = (c >= 0) ? 2 * c : c;
+      }
+  }
+  if(leaf_ids) GSQ_CUDA_TRY(cudaMemcpy(leaf_ids, h->dev.perm, sizeof(int) * n, cudaMemcpyDeviceToHost));
+  if(codes) GSQ_CUDA_TRY(cudaMemcpy(codes, h->dev.codes, sizeof(uint32_t) * n, cudaMemcpyDeviceToHost));
+  return GSQ_OK;
+}
+
+}  // extern "C"
+
+namespace gsq
+{
+// Accessor for the signed-distance translation unit.
+const BvhDev* bvh_dev(const gsq_bvh* h) { return h ? &h->dev : nullptr; }
+gsq_bvh* bvh_new_internal(int device)
+{
+  gsq_bvh* h = nullptr;
+  if(gsq_bvh_create(&h) != GSQ_OK) return nullptr;
+  h->device = device;
+  return h;
+}
+int bvh_build_internal(gsq_bvh* h, const double* d_boxes, int n, cudaStream_t s)
+{
+  h->built = false;
+  const int rc = bvh_build(h->dev, d_boxes, n, h->scale, s, h->d_err);
+  if(rc == GSQ_OK) h->built = true;
+  return rc;
+}
+}  // namespace gsq

@@ -1,0 +1,203 @@
+// Internal declarations shared by the libgsq translation units.
+//
+// Device-side geometry helpers here keep the operation order of the axom
+// primitives they restate (cited per function); the library is compiled with
+// -fmad=false so no multiply-add is contracted, which keeps FP64 results
+// bit-identical to the reference's host build.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <cfloat>
+#include <cstdint>
+#include <string>
+
+#include "../../include/gsq.h"
+
+namespace gsq
+{
+// ---- error reporting ------------------------------------------------------
+void set_error(const std::string& msg);
+int fail(int code, const std::string& msg);
+int cuda_fail(cudaError_t e, const char* what);
+
+#define GSQ_CUDA_TRY(expr)                              \
+  do                                                    \
+  {                                                     \
+    cudaError_t e_ = (expr);                            \
+    if(e_ != cudaSuccess) return ::gsq::cuda_fail(e_, #expr); \
+  } while(0)
+
+// Device-side error flags (bit set by kernels, read by the host after a sync).
+enum DeviceError : int
+{
+  DEVERR_STACK = 1,      // traversal stack overflow
+  DEVERR_WAIT = 2,       // a bounded spin-wait expired
+  DEVERR_RANGE = 4,      // an index was out of range
+};
+
+// True if ptr is device (or managed) memory of some device.
+bool is_device_ptr(const void* ptr);
+
+// Adds n to the library-wide count of kernel launches (gsq_kernel_launches).
+void count_launch(int n = 1);
+
+// ---- stream-ordered scratch -----------------------------------------------
+// Owns one cudaMallocAsync allocation, freed on the same stream.
+struct Scratch
+{
+  void* p = nullptr;
+  cudaStream_t s = nullptr;
+  Scratch() = default;
+  Scratch(const Scratch&) = delete;
+  Scratch& operator=(const Scratch&) = delete;
+  ~Scratch() { release(); }
+  cudaError_t alloc(size_t bytes, cudaStream_t stream)
+  {
+    release();
+    s = stream;
+    return cudaMallocAsync(&p, bytes ? bytes : 16, stream);
+  }
+  void release()
+  {
+    if(p) cudaFreeAsync(p, s);
+    p = nullptr;
+  }
+  template <class T>
+  T* as() const
+  {
+    return static_cast<T*>(p);
+  }
+};
+
+// Device buffer that is either the caller's device pointer or a staged copy
+// of the caller's host array.
+struct InBuf
+{
+  const void* dev = nullptr;
+  Scratch own;
+  cudaError_t stage(const void* user, size_t bytes, cudaStream_t s)
+  {
+    if(user == nullptr || bytes == 0 || is_device_ptr(user))
+    {
+      dev = user;
+      return cudaSuccess;
+    }
+    cudaError_t e = own.alloc(bytes, s);
+    if(e != cudaSuccess) return e;
+    dev = own.p;
+    return cudaMemcpyAsync(own.p, user, bytes, cudaMemcpyHostToDevice, s);
+  }
+};
+
+// Device buffer for an output that may be host memory (copied back by flush).
+struct OutBuf
+{
+  void* user = nullptr;
+  void* dev = nullptr;
+  size_t bytes = 0;
+  Scratch own;
+  cudaError_t prepare(void* u, size_t b, cudaStream_t s)
+  {
+    user = u;
+    bytes = b;
+    if(u == nullptr || b == 0 || is_device_ptr(u))
+    {
+      dev = u;
+      return cudaSuccess;
+    }
+    cudaError_t e = own.alloc(b, s);
+    dev = own.p;
+    return e;
+  }
+  cudaError_t flush(cudaStream_t s)
+  {
+    if(user && dev != user && bytes) return cudaMemcpyAsync(user, dev, bytes, cudaMemcpyDeviceToHost, s);
+    return cudaSuccess;
+  }
+};
+
+// ---- layouts ----------------------------------------------------------------
+// One record per inner node i: boxes of its two children (AoS lo/hi, left
+// then right) and their links: c >= 0 an inner node, -(leafpos+1) a leaf.
+// 128 bytes, one cache line per node visit.
+struct __align__(16) NodeRec64
+{
+  double b[12];  // lo_l[3] hi_l[3] lo_r[3] hi_r[3]
+  int child[2];
+  int pad[6];
+};
+static_assert(sizeof(NodeRec64) == 128, "node record must be one 128-byte line");
+
+// FP32 copy of a node record, boxes rounded outward (lo down, hi up). 64 B.
+struct __align__(16) NodeRec32
+{
+  float b[12];
+  int child[2];
+  int pad[2];
+};
+static_assert(sizeof(NodeRec32) == 64, "fp32 node record must be 64 bytes");
+
+constexpr int STACK_SIZE = 64;            // bvh_traverse.hpp:79
+constexpr int BARRIER = -2000000000;      // bvh_traverse.hpp:80
+constexpr double DEFAULT_SCALE = 1.000123;  // spin/BVH.hpp:410
+
+// Built hierarchy resident in device memory.
+struct BvhDev
+{
+  int n = 0;                      // leaves (>= 2 once built)
+  NodeRec64* nodes = nullptr;     // n-1 records (root = 0)
+  int* perm = nullptr;            // sorted leaf position -> original id
+  uint32_t* codes = nullptr;      // sorted Morton codes
+  int* lchild = nullptr;          // radix tree links (kept for export)
+  int* rchild = nullptr;
+  double bounds[6];               // host copy of the global bounds
+  void* block = nullptr;          // single allocation backing the arrays
+  size_t block_bytes = 0;
+  void release();
+};
+
+// Builds the hierarchy over n boxes (device array, n x 6), padding 0/1 boxes
+// to 2 like BVH::initialize.  Returns a GSQ status.
+int bvh_build(BvhDev& B, const double* d_boxes, int n, double scale, cudaStream_t s, int* d_err);
+
+// Stable LSD radix sort of (key, value) pairs on key bits [0, end_bit).
+// Inputs in keys[0]/vals[0]; keys[1]/vals[1] are scratch of the same size.
+// If vals_iota, vals[0] is ignored and the values start as 0..n-1.  Returns
+// the index (0 or 1) of the buffers holding the result, or a negative GSQ
+// status.  d_err gets DEVERR_WAIT if a look-back wait expired.
+int radix_sort_pairs(uint32_t* keys[2], int* vals[2], int n, int end_bit, bool vals_iota, cudaStream_t s,
+                     int* d_err);
+
+// Exclusive scan of m int32 counts into offsets; *d_total (device int64)
+// receives the sum.
+int exclusive_scan(const int* d_in, int* d_out, int m, long long* d_total, cudaStream_t s);
+
+// Reads and clears the device error word; returns a GSQ status.
+int check_device_error(int* d_err, cudaStream_t s, const char* what);
+
+// ---- exact device geometry (restatements of axom primal) ----------------
+struct DBox
+{
+  double lo[3], hi[3];
+};
+
+__host__ __device__ inline bool box_valid(const double* lo, const double* hi)
+{
+  // BoundingBox::isValid (primal/geometry/BoundingBox.hpp:451-460)
+  return !(lo[0] > hi[0] || lo[1] > hi[1] || lo[2] > hi[2]);
+}
+
+__host__ __device__ inline double dot3(double u0, double u1, double u2, double v0, double v1, double v2)
+{
+  // Vector::dot_product (primal/geometry/Vector.hpp:544-553): accumulator
+  // starts at 0, so (0 + u0 v0) + u1 v1 + u2 v2.
+  double r = 0.0;
+  r = r + u0 * v0;
+  r = r + u1 * v1;
+  r = r + u2 * v2;
+  return r;
+}
+
+__host__ __device__ inline bool near_eq(double a, double b, double eps) { return fabs(a - b) <= eps; }
+
+}  // namespace gsq

@@ -68,6 +68,32 @@ def icosphere(level: int) -> tuple[np.ndarray, np.ndarray]:
     return v, f.astype(np.int32)
 
 
+def quad_sphere(n: int) -> tuple[np.ndarray, np.ndarray]:
+    """Cube with n x n quads per face projected to the unit sphere: (V,3), (6n^2, 4).
+
+    Quads are wound counter-clockwise seen from outside."""
+    e = np.eye(3)
+    faces = [(np.array([1., -1, -1]), 2 * e[1], 2 * e[2]), (np.array([-1., -1, -1]), 2 * e[2], 2 * e[1]),
+             (np.array([-1., 1, -1]), 2 * e[2], 2 * e[0]), (np.array([-1., -1, -1]), 2 * e[0], 2 * e[2]),
+             (np.array([-1., -1, 1]), 2 * e[0], 2 * e[1]), (np.array([-1., -1, -1]), 2 * e[1], 2 * e[0])]
+    t = np.arange(n + 1) / n
+    pts, quads = [], []
+    for k, (o, u, w) in enumerate(faces):
+        I, J = np.meshgrid(t, t, indexing="ij")
+        pts.append(o + I[..., None] * u + J[..., None] * w)
+        base = k * (n + 1) ** 2
+        i, j = np.meshgrid(np.arange(n), np.arange(n), indexing="ij")
+        idx = lambda a, b: base + a * (n + 1) + b  # noqa: E731
+        quads.append(np.stack([idx(i, j), idx(i + 1, j), idx(i + 1, j + 1), idx(i, j + 1)], -1).reshape(-1, 4))
+    p = np.concatenate([q.reshape(-1, 3) for q in pts])
+    quads = np.concatenate(quads)
+    key = np.round(p * 4 * n).astype(np.int64)
+    _, first, inv = np.unique(key, axis=0, return_index=True, return_inverse=True)
+    v = p[first]
+    v /= np.linalg.norm(v, axis=1, keepdims=True)
+    return v, inv.reshape(-1)[quads].astype(np.int32)
+
+
 def displace(v: np.ndarray, seed: int, amp: float = 0.1, terms: int = 8) -> np.ndarray:
     g = rng(seed)
     mk = g.integers(1, 7, size=terms)

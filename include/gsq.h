@@ -1,0 +1,192 @@
+/*
+ * gsq.h -- C ABI of the GB300-native spatial-query library (libgsq.so).
+ *
+ * Drop-in boundary for LLNL/axom's spatial-query hot path:
+ *   - spin::BVH<3, Exec, double>           (src/axom/spin/BVH.hpp:129-568)
+ *   - quest::SignedDistance<3, Exec>       (src/axom/quest/SignedDistance.hpp:147-605)
+ *   - the quest C API / shroud wrappers     (src/axom/quest/interface/signed_distance.hpp:88-319,
+ *                                            src/axom/quest/interface/c_fortran/wrapQUEST.h:84-129)
+ *
+ * Conventions
+ *   - Every function returns an int status: GSQ_OK (0) on success, a negative
+ *     GSQ_ERR_* code otherwise; gsq_last_error() describes the last failure of
+ *     the calling thread.  Nothing aborts (the reference's SLIC_ERROR does).
+ *   - Coordinates are IEEE double.  Indices and counts are int32, as axom's
+ *     default IndexType (src/cmake/AxomOptions.cmake:25).
+ *   - Array arguments may live in host memory or in device memory of the
+ *     current CUDA device; each pointer is classified on entry.  Host inputs
+ *     are staged to the device and device results copied back to host outputs.
+ *   - `stream` is a cudaStream_t passed as void* (NULL = legacy default
+ *     stream).  Calls are synchronous with respect to that stream, like the
+ *     reference's SYNCHRONOUS execution policies: outputs are complete when the
+ *     call returns.
+ *   - Boxes are 6 doubles {xmin, ymin, zmin, xmax, ymax, zmax}, the memory
+ *     layout of primal::BoundingBox<double,3> (BoundingBox.hpp:363-367), so an
+ *     array of reference boxes can be passed as is.  Points are 3 doubles, the
+ *     layout of primal::Point<double,3>.
+ *   - Device work runs on the CUDA device that is current when the handle is
+ *     created; a handle must be used with that device current.
+ */
+#ifndef GSQ_H_
+#define GSQ_H_
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes ---------------------------------------------------- */
+#define GSQ_OK 0
+#define GSQ_ERR_INVALID -1  /* bad argument; also BVH_BUILD_FAILED (spin/BVH.hpp:39-43) */
+#define GSQ_ERR_CUDA -2     /* a CUDA runtime call failed */
+#define GSQ_ERR_NOMEM -3    /* device or host allocation failed */
+#define GSQ_ERR_DEVICE -4   /* a kernel reported an error (stack overflow, bounded wait expired) */
+#define GSQ_ERR_STATE -5    /* call out of order (e.g. query before build) */
+
+/* Precision forms of the signed-distance query. */
+#define GSQ_PRECISION_FP64 0  /* op-for-op FP64 restatement of the reference */
+#define GSQ_PRECISION_MIXED 1 /* FP32 outward-rounded traversal, FP64 refine and sign */
+
+typedef struct gsq_bvh gsq_bvh;
+typedef struct gsq_sdf gsq_sdf;
+
+/* Message of the last failed call on this thread ("" if none). */
+const char* gsq_last_error(void);
+
+/* Library version string. */
+const char* gsq_version(void);
+
+/* Number of CUDA kernels this library has launched in this process (for
+ * launch accounting in benchmarks).  No reference counterpart. */
+int64_t gsq_kernel_launches(void);
+
+/* Frees a candidate array returned by a gsq_bvh_find_* call, wherever it lives. */
+int gsq_free(void* ptr);
+
+/* Copies bytes between any two host or device pointers (cudaMemcpyDefault),
+ * e.g. a device candidate array into a caller buffer.  No reference
+ * counterpart: axom::copy (core/memory_management.hpp) plays this role there. */
+int gsq_memcpy(void* dst, const void* src, size_t bytes);
+
+/* ---- spin::BVH -------------------------------------------------------- */
+
+/* Replaces spin::BVH::BVH() (spin/BVH.hpp:185); default scale factor
+ * 1.000123 and tolerance DBL_EPSILON (spin/BVH.hpp:410-412). */
+int gsq_bvh_create(gsq_bvh** out);
+int gsq_bvh_destroy(gsq_bvh* bvh);
+
+/* Replaces BVH::setScaleFactor / getScaleFactor (spin/BVH.hpp:269-275). */
+int gsq_bvh_set_scale_factor(gsq_bvh* bvh, double scale);
+int gsq_bvh_get_scale_factor(const gsq_bvh* bvh, double* scale);
+/* Replaces BVH::setTolerance / getTolerance (spin/BVH.hpp:283-289); the
+ * tolerance is the ray test's near-zero direction threshold. */
+int gsq_bvh_set_tolerance(gsq_bvh* bvh, double tol);
+int gsq_bvh_get_tolerance(const gsq_bvh* bvh, double* tol);
+
+/* Replaces BVH::initialize(boxes, numItems) (spin/BVH.hpp:424-477):
+ * Morton codes, stable radix sort, Karras hierarchy, bottom-up refit.
+ * boxes: n x 6 doubles.  n may be 0 or 1 (padded as the reference does). */
+int gsq_bvh_build(gsq_bvh* bvh, const double* boxes, int32_t n, void* stream);
+
+/* Replaces BVH::getBounds (spin/BVH.hpp:297-309): global bounds of the
+ * scaled input boxes.  lo/hi are host arrays of 3. */
+int gsq_bvh_bounds(const gsq_bvh* bvh, double* lo, double* hi);
+
+/* Number of leaves stored (after padding of 0/1 boxes to 2). */
+int gsq_bvh_num_leaves(const gsq_bvh* bvh, int32_t* n);
+
+/* Candidate queries.  Replace BVH::findBoundingBoxes / findPoints / findRays
+ * (spin/BVH.hpp:480-568, policy/LinearBVH.hpp:271-402).
+ *   offsets, counts : m int32 each, caller-owned (host or device).
+ *   *candidates     : allocated by the library in the memory space of
+ *                     `offsets` (free with gsq_free); query i's candidate ids
+ *                     are candidates[offsets[i] .. offsets[i]+counts[i]).
+ *   total           : host int64, the number of candidates (nullable).
+ * Candidate order within a query is the reference traversal order. */
+int gsq_bvh_find_boxes(const gsq_bvh* bvh, const double* query_boxes, int32_t m, int32_t* offsets,
+                       int32_t* counts, int32_t** candidates, int64_t* total, void* stream);
+/* points: m x 3 doubles. */
+int gsq_bvh_find_points(const gsq_bvh* bvh, const double* points, int32_t m, int32_t* offsets,
+                        int32_t* counts, int32_t** candidates, int64_t* total, void* stream);
+/* origins, directions: m x 3 doubles.  Directions are the rays' stored unit
+ * directions, as primal::Ray keeps them (primal/geometry/Ray.hpp:123-128);
+ * gsq_ray_normalize gives the same normalisation for raw directions. */
+int gsq_bvh_find_rays(const gsq_bvh* bvh, const double* origins, const double* directions, int32_t m,
+                      int32_t* offsets, int32_t* counts, int32_t** candidates, int64_t* total, void* stream);
+
+/* Host helper: primal::Vector::unitVector (primal/geometry/Vector.hpp:477-493)
+ * applied to m raw directions (host arrays, m x 3). */
+int gsq_ray_normalize(const double* raw, int32_t m, double* unit);
+
+/* Debug export of the built hierarchy in the reference's LinearBVH layout
+ * (policy/LinearBVH.hpp:170-188, 225-266), to host arrays (each nullable):
+ *   node_boxes   2(n-1) x 6 : child boxes of inner node i at rows 2i, 2i+1
+ *   children     2(n-1)     : 2*c for inner child c, -(leafpos+1) for a leaf
+ *   leaf_ids     n          : original box id of each sorted leaf position
+ *   codes        n          : sorted Morton codes (build_radix_tree.hpp:146-260)
+ * where n = gsq_bvh_num_leaves. */
+int gsq_bvh_export(const gsq_bvh* bvh, double* node_boxes, int32_t* children, int32_t* leaf_ids,
+                   uint32_t* codes);
+
+/* Milliseconds of device time taken by the last gsq_bvh_build on this
+ * handle (CUDA events around the build's kernels). */
+int gsq_bvh_last_build_ms(const gsq_bvh* bvh, float* ms);
+
+/* ---- quest::SignedDistance --------------------------------------------- */
+
+typedef struct gsq_sdf_opts {
+  int32_t precision;      /* GSQ_PRECISION_FP64 (default) or GSQ_PRECISION_MIXED */
+  int32_t sort_queries;   /* 1: process queries in Morton order (default 1) */
+  int32_t block_size;     /* threads per block of the query kernel (0 = default) */
+  int32_t reserved[5];
+} gsq_sdf_opts;
+
+/* Fills opts with the defaults. */
+int gsq_sdf_opts_init(gsq_sdf_opts* opts);
+
+/* Replaces SignedDistance(const mint::Mesh*, isWatertight, computeSign)
+ * and setMesh (quest/SignedDistance.hpp:410-504): mesh box, per-cell boxes
+ * and the BVH build.  The mesh is an unstructured single-shape surface mesh:
+ *   x, y, z         : nverts node coordinates
+ *   cells           : ncells x nodes_per_cell node ids (int32)
+ *   nodes_per_cell  : 3 (triangles) or 4 (quads, split as the reference does)
+ * The handle keeps its own device copy of the mesh (the reference borrows
+ * the mint mesh).  opts nullable. */
+int gsq_sdf_create(gsq_sdf** out, const double* x, const double* y, const double* z, int32_t nverts,
+                   const int32_t* cells, int32_t ncells, int32_t nodes_per_cell, int32_t watertight,
+                   int32_t compute_sign, const gsq_sdf_opts* opts, void* stream);
+int gsq_sdf_destroy(gsq_sdf* sdf);
+
+/* Changes the options of an existing handle (precision, query order, ...). */
+int gsq_sdf_set_opts(gsq_sdf* sdf, const gsq_sdf_opts* opts);
+
+/* Replaces SignedDistance::computeDistances(npts, queryPts, outSgnDist,
+ * outClosestPts, outNormals) (quest/SignedDistance.hpp:527-605) and the C
+ * API's signed_distance_evaluate (quest/interface/signed_distance.hpp:290,
+ * quest/interface/signed_distance.cpp:432-465).
+ *   qx, qy, qz : query coordinates; element i is q*[i * stride]
+ *                (stride 1 = three SoA arrays, as ZipPoint / the C API;
+ *                 stride 3 with qy = qx+1, qz = qx+2 = an array of points)
+ *   out        : m signed distances
+ *   closest    : m x 3 closest points (nullable)
+ *   normals    : m x 3 unit pseudo-normals (nullable) */
+int gsq_sdf_eval(const gsq_sdf* sdf, const double* qx, const double* qy, const double* qz, int32_t stride,
+                 int32_t m, double* out, double* closest, double* normals, void* stream);
+
+/* Replaces signed_distance_get_mesh_bounds (quest/interface/signed_distance.hpp:308):
+ * bounding box of the mesh nodes (host lo[3], hi[3]). */
+int gsq_sdf_mesh_bounds(const gsq_sdf* sdf, double* lo, double* hi);
+
+/* The BVH built over the mesh cells (SignedDistance::getBVHTree,
+ * quest/SignedDistance.hpp:337).  Owned by the sdf handle. */
+int gsq_sdf_get_bvh(const gsq_sdf* sdf, const gsq_bvh** bvh);
+
+/* Milliseconds of device time of the last gsq_sdf_eval's query kernel. */
+int gsq_sdf_last_eval_ms(const gsq_sdf* sdf, float* ms);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* GSQ_H_ */

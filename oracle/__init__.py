@@ -45,11 +45,12 @@ def build_port(force: bool = False) -> Path:
     return PORT_LIB
 
 
-def build_ref(reference: Path = DEFAULT_REFERENCE) -> Path | None:
+def build_reference(reference: Path = DEFAULT_REFERENCE) -> Path | None:
     """Build the reference's own SEQ path when its sources are present."""
     if not (reference / "src/axom/spin/BVH.hpp").exists():
         return None
-    from . import build_ref as br
+    import importlib
+    br = importlib.import_module(__name__ + ".build_ref")
     return br.build(reference, os.cpu_count() or 4)
 
 
@@ -227,14 +228,15 @@ class Ref(_Lib):
             raise FileNotFoundError(path)
         super().__init__(path)
         L = self.lib
-        L.ref_sdf_create.argtypes = [_dp, _dp, _dp, C.c_int, _ip, C.c_int, C.c_int, C.c_int]
+        L.ref_sdf_create.argtypes = [_dp, _dp, _dp, C.c_int, _ip, C.c_int, C.c_int, C.c_int, C.c_int]
         L.ref_bvh_find_rays.restype = C.c_longlong
         L.ref_bvh_find_rays.argtypes = [C.c_void_p, _dp, _dp, C.c_int, _ip, _ip, C.POINTER(_ip), _dp]
 
     def sdf(self, x, y, z, cells, watertight=True, compute_sign=True):
         x, y, z = (_arr(a, np.float64) for a in (x, y, z))
-        cells = _arr(cells, np.int32).reshape(-1, 3)
-        h = self.lib.ref_sdf_create(_p(x), _p(y), _p(z), x.size, _p(cells), cells.shape[0],
+        cells = _arr(cells, np.int32)
+        npc = cells.shape[1] if cells.ndim == 2 else 3
+        h = self.lib.ref_sdf_create(_p(x), _p(y), _p(z), x.size, _p(cells), cells.size // npc, npc,
                                     int(watertight), int(compute_sign))
         return _Handle(self, h, "sdf_destroy")
 

@@ -209,8 +209,9 @@ void* ref_sdf_create(const double* x,
                      const double* y,
                      const double* z,
                      int nverts,
-                     const int* tris,
-                     int ntris,
+                     const int* cells,
+                     int ncells,
+                     int nodes_per_cell,
                      int watertight,
                      int compute_sign)
 {
@@ -219,8 +220,14 @@ void* ref_sdf_create(const double* x,
   h->x.assign(x, x + nverts);
   h->y.assign(y, y + nverts);
   h->z.assign(z, z + nverts);
-  h->conn.assign(tris, tris + 3 * (long long)ntris);
-  h->mesh = new UMesh(axom::mint::TRIANGLE, ntris, h->conn.data(), nverts, h->x.data(), h->y.data(), h->z.data());
+  h->conn.assign(cells, cells + (long long)nodes_per_cell * ncells);
+  h->mesh = new UMesh(nodes_per_cell == 4 ? axom::mint::QUAD : axom::mint::TRIANGLE,
+                      ncells,
+                      h->conn.data(),
+                      nverts,
+                      h->x.data(),
+                      h->y.data(),
+                      h->z.data());
   h->sd = new SDType(h->mesh, watertight != 0, compute_sign != 0);
   return h;
 }

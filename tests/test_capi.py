@@ -1,0 +1,74 @@
+"""CPU: libgsq.so builds, loads, and exports every symbol include/gsq.h declares.
+
+No compute call needs a GPU here; only argument validation and the host
+helpers run.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import re
+
+import numpy as np
+import pytest
+
+from conftest import ROOT, assert_bits_equal, golden
+
+
+@pytest.fixture(scope="module")
+def lib():
+    from axom_gb300 import build
+    build.build()
+    import axom_gb300
+    return axom_gb300.load()
+
+
+def declared_functions() -> list[str]:
+    names = []
+    for h in (ROOT / "include").glob("*.h"):
+        text = re.sub(r"/\*.*?\*/", "", h.read_text(), flags=re.S)
+        names += re.findall(r"^\s*(?:const\s+)?\w+\**\s+\**(gsq_\w+)\s*\(", text, flags=re.M)
+    return sorted(set(names))
+
+
+def test_header_declares_entry_points():
+    names = declared_functions()
+    for must in ("gsq_bvh_build", "gsq_bvh_find_boxes", "gsq_bvh_find_points", "gsq_bvh_find_rays",
+                 "gsq_sdf_create", "gsq_sdf_eval"):
+        assert must in names
+
+
+def test_library_exports_every_declared_symbol(lib):
+    missing = [n for n in declared_functions() if not hasattr(lib, n)]
+    assert not missing, f"symbols declared but not exported: {missing}"
+
+
+def test_python_signatures_cover_header():
+    import axom_gb300
+    bound = {n for n, _, _ in axom_gb300.SIGNATURES}
+    missing = [n for n in declared_functions() if n not in bound]
+    assert not missing, f"entry points without a Python binding: {missing}"
+
+
+def test_argument_validation_without_gpu(lib):
+    assert lib.gsq_bvh_create(None) == -1
+    assert b"null" in lib.gsq_last_error()
+    assert lib.gsq_bvh_set_scale_factor(None, 1.0) == -1
+    assert lib.gsq_sdf_create(None, None, None, None, 0, None, 0, 3, 1, 1, None, None) == -1
+    assert lib.gsq_sdf_eval(None, None, None, None, 1, 1, None, None, None, None) == -1
+    assert lib.gsq_free(None) == 0
+    assert lib.gsq_version().startswith(b"gsq")
+
+
+def test_ray_normalize_matches_reference(lib):
+    import axom_gb300
+    g = golden("bvh_boxes2000")
+    assert_bits_equal(axom_gb300.normalize_rays(g["ray_dirs_raw"]), g["ray_dirs"], "ray directions")
+    z = axom_gb300.normalize_rays(np.zeros((1, 3)))
+    assert np.array_equal(z, [[1.0, 0.0, 0.0]])
+
+
+def test_opts_defaults(lib):
+    import axom_gb300
+    o = axom_gb300.SdfOpts()
+    assert lib.gsq_sdf_opts_init(C.byref(o)) == 0
+    assert o.precision == 0 and o.sort_queries == 1

@@ -1,0 +1,184 @@
+"""CPU: the oracle (C++ restatement) pinned against the reference and its tests.
+
+* bit-exact against the committed golden fixtures (made by running the
+  reference, tests/golden/make_golden.py);
+* bit-exact against the reference library itself, live, where it is built;
+* the reference's own known-answer tests (spin/tests/spin_bvh.cpp,
+  quest/tests/quest_signed_distance.cpp, quest_signed_distance_interface.cpp).
+"""
+from __future__ import annotations
+
+import numpy as np
+import pytest
+
+from axom_gb300 import workloads as W
+from conftest import assert_bits_equal, golden
+
+SCALES = [(1.000123, "s"), (1.0, "u")]
+
+
+@pytest.mark.parametrize("scale,tag", SCALES)
+def test_port_build_matches_golden(port, scale, tag):
+    g = golden("bvh_boxes2000")
+    it = port.internals(g["boxes"], scale)
+    for k in ("codes", "perm", "lchild", "rchild", "parents", "inner", "bounds"):
+        assert_bits_equal(it[k], g[f"{tag}_{k}"], k)
+
+
+@pytest.mark.parametrize("scale,tag", SCALES)
+def test_port_find_matches_golden(port, scale, tag):
+    g = golden("bvh_boxes2000")
+    h = port.bvh(g["boxes"], scale)
+    assert_bits_equal(port.bounds(h), g[f"{tag}_bvh_bounds"], "bounds")
+    for key, res in (("fb", port.find_boxes(h, g["query_boxes"])), ("fp", port.find_points(h, g["points"])),
+                     ("fr", port.find_rays(h, g["ray_origins"], g["ray_dirs"]))):
+        for name, arr in zip(("offsets", "counts", "candidates"), res):
+            assert_bits_equal(arr, g[f"{tag}_{key}_{name}"], f"{key} {name}")
+
+
+def test_port_ray_normalisation_matches_golden(port):
+    g = golden("bvh_boxes2000")
+    assert_bits_equal(port.normalize_rays(g["ray_dirs_raw"]), g["ray_dirs"], "ray dirs")
+
+
+@pytest.mark.parametrize("name", ["sdf_uvsphere", "sdf_ico3", "sdf_ico3_open", "sdf_ico3_unsigned", "sdf_quad12"])
+def test_port_sdf_matches_golden(port, name):
+    g = golden(name)
+    v = g["vertices"]
+    h = port.sdf(v[:, 0], v[:, 1], v[:, 2], g["cells"], bool(g["watertight"]), bool(g["sign"]))
+    d, cp, nr = port.sdf_eval(h, g["queries"], True, True)
+    assert_bits_equal(d, g["dist"], "distance")
+    assert_bits_equal(cp, g["closest"], "closest point")
+    np.testing.assert_allclose(nr, g["normals"], rtol=0, atol=1e-12)
+    assert_bits_equal(port.mesh_bounds(h), g["mesh_bounds"], "mesh bounds")
+    if "box_tests" in g:
+        nb, nl = port.sdf_counts(h, g["queries"])
+        assert_bits_equal(nb, g["box_tests"], "box tests")
+        assert_bits_equal(nl, g["leaf_tests"], "leaf tests")
+
+
+def test_sphere_norms_match_reference_test():
+    """quest_signed_distance.cpp:86-169: l1, l2, linf against the analytic sphere."""
+    g = golden("sdf_uvsphere")
+    phi = g["dist"]
+    exact = np.linalg.norm(g["queries"], axis=1) - 0.5
+    diff = phi - exact
+    assert np.all(np.abs(diff) <= 1e-2)
+    l1 = np.sum(np.abs(diff))
+    l2 = np.sqrt(np.sum(diff))
+    linf = np.max(np.abs(diff))
+    assert abs(l1 - 6.7051997372579715) <= 1e-3
+    assert abs(l2 - 2.5894400431865519) <= 1e-3
+    assert abs(linf - 0.00532092) <= 1e-3
+
+
+def _uniform_cells_3x3x3():
+    return W.uniform_cells([0.0, 0.0, 0.0], [3.0, 3.0, 3.0], 4)
+
+
+def test_known_answers_find_boxes(port):
+    """spin_bvh.cpp:279-406: query box 0 hits cells 0-17, query box 1 hits none."""
+    h = port.bvh(_uniform_cells_3x3x3(), 1.0)
+    lo, hi = port.bounds(h)[:3], port.bounds(h)[3:]
+    np.testing.assert_allclose(lo, 0.0, atol=1e-12)
+    np.testing.assert_allclose(hi, 3.0, atol=1e-12)
+    q = np.array([[-1.0, -1, -1, 2.5, 2.5, 1.5], [-1.0, -1, -1, -0.5, -0.5, -0.5]])
+    off, cnt, cand = port.find_boxes(h, q)
+    assert list(cnt) == [18, 0]
+    assert sorted(cand[off[0]:off[0] + 18]) == list(range(18))
+
+
+def test_known_answers_find_rays(port):
+    """spin_bvh.cpp:519-648: the diagonal ray hits 15 listed cells, the opposite ray none."""
+    h = port.bvh(_uniform_cells_3x3x3(), 1.0)
+    o = np.array([[-1.0, -1, -1], [-1.0, -1, -1]])
+    d = port.normalize_rays(np.array([[1.0, 1, 1], [-1.0, -1, -1]]))
+    off, cnt, cand = port.find_rays(h, o, d)
+    assert list(cnt) == [15, 0]
+    assert sorted(cand) == [0, 1, 3, 4, 9, 10, 12, 13, 14, 16, 17, 22, 23, 25, 26]
+
+
+def test_known_answers_find_points(port):
+    """spin_bvh.cpp:792-903: each centroid hits exactly its cell; shifted points hit none."""
+    cells = _uniform_cells_3x3x3()
+    h = port.bvh(cells, 1.0)
+    cent = 0.5 * (cells[:, :3] + cells[:, 3:])
+    off, cnt, cand = port.find_points(h, cent)
+    assert np.all(cnt == 1)
+    assert np.array_equal(cand[off], np.arange(27))
+    off, cnt, cand = port.find_points(h, cent + 10.0)
+    assert np.all(cnt == 0)
+
+
+def plane_mesh():
+    """The 4-triangle open plane of quest_signed_distance_interface.cpp:61-108."""
+    v = np.array([[-5.0, -5, 0], [5, -5, 0], [0, 0, 0], [5, 5, 0], [-5, 5, 0]])
+    f = np.array([[0, 1, 2], [1, 3, 2], [3, 4, 2], [4, 0, 2]], np.int32)
+    return v, f
+
+
+def test_known_answers_plane(port):
+    """quest_signed_distance_interface.cpp:186-242: exact distance to the plane z = 0."""
+    v, f = plane_mesh()
+    h = port.sdf(v[:, 0], v[:, 1], v[:, 2], f, watertight=False)
+    q = W.uniform_grid([-4.0] * 3, [4.0] * 3, 16)
+    d, _, _ = port.sdf_eval(h, q)
+    np.testing.assert_array_max_ulp(d, q[:, 2], maxulp=4)
+
+
+@pytest.mark.parametrize("n", [1, 2, 3, 5, 17, 200])
+def test_port_matches_reference_small(port, ref, n):
+    boxes = W.random_boxes(n, 40 + n)
+    if n >= 2:
+        a, b = port.internals(boxes), ref.internals(boxes)
+        for k in a:
+            assert_bits_equal(a[k], b[k], k)
+    hp, hr = port.bvh(boxes), ref.bvh(boxes)
+    assert_bits_equal(port.bounds(hp), ref.bounds(hr), "bounds")
+    q = W.random_boxes(300, 7)
+    for x, y in zip(port.find_boxes(hp, q), ref.find_boxes(hr, q)):
+        assert_bits_equal(x, y, "find boxes")
+
+
+def test_port_matches_reference_edge_cases(port, ref):
+    """Duplicate boxes (all Morton ties), invalid boxes, points as boxes, signed zeros."""
+    rng = np.random.default_rng(3)
+    dup = np.tile(W.random_boxes(1, 1), (64, 1))
+    inval = W.random_boxes(50, 2)
+    inval[::3, [0, 3]] = inval[::3, [3, 0]]  # min > max on x: invalid
+    pts = rng.uniform(-1, 1, (40, 3))
+    degen = np.concatenate([pts, pts], 1)
+    zeros = np.zeros((8, 6))
+    zeros[::2] = -0.0
+    zeros[1::4, 3:] = 1.0
+    for boxes in (dup, inval, degen, zeros, np.concatenate([dup, inval, degen, zeros])):
+        for scale in (1.000123, 1.0):
+            a, b = port.internals(boxes, scale), ref.internals(boxes, scale)
+            for k in a:
+                assert_bits_equal(a[k], b[k], k)
+            hp, hr = port.bvh(boxes, scale), ref.bvh(boxes, scale)
+            q = np.concatenate([boxes[:20], W.random_boxes(20, 9) * 2 - 1])
+            for x, y in zip(port.find_boxes(hp, q), ref.find_boxes(hr, q)):
+                assert_bits_equal(x, y, "find boxes")
+
+
+def test_port_matches_reference_sdf_live(port, ref):
+    v, f = W.displaced_icosphere(4, 77)
+    q = W.mixed_queries(v, f, 3000, 5)
+    for wt, sg in ((True, True), (False, True), (True, False)):
+        hp = port.sdf(v[:, 0], v[:, 1], v[:, 2], f, wt, sg)
+        hr = ref.sdf(v[:, 0], v[:, 1], v[:, 2], f, wt, sg)
+        a = port.sdf_eval(hp, q, True, True)
+        b = ref.sdf_eval(hr, q, True, True)
+        assert_bits_equal(a[0], b[0], "distance")
+        assert_bits_equal(a[1], b[1], "closest")
+        assert_bits_equal(a[2], b[2], "normals")
+
+
+def test_port_threads_are_deterministic(port):
+    v, f = W.displaced_icosphere(3, 1)
+    q = W.uniform_queries(v, 4000, 2)
+    h = port.sdf(v[:, 0], v[:, 1], v[:, 2], f)
+    a = port.sdf_eval(h, q, threads=1)[0]
+    b = port.sdf_eval(h, q, threads=4)[0]
+    assert_bits_equal(a, b, "threads")
