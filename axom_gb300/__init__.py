@@ -311,11 +311,13 @@ class SignedDistance:
         self._opts.sort_queries = int(on)
         _check(self._lib.gsq_sdf_set_opts(self._h, C.byref(self._opts)))
 
-    def compute_distances(self, points, closest: bool = False, normals: bool = False):
-        """Signed distances of (m, 3) points; optional closest points and unit normals."""
+    def compute_distances(self, points, closest: bool = False, normals: bool = False, out=None):
+        """Signed distances of (m, 3) points; optional closest points and unit normals.
+
+        ``out`` (optional) is a caller-owned (m,) float64 buffer, host or device."""
         p = _Arr(points, np.float64, 3)
         m = p.n
-        out = p.empty(m, np.float64)
+        out = p.empty(m, np.float64) if out is None else out
         cp = p.empty((m, 3), np.float64) if closest else None
         nr = p.empty((m, 3), np.float64) if normals else None
         base = p.ptr

@@ -1,0 +1,313 @@
+"""Benchmark: signed-distance queries/s against a 1.3M-triangle mesh on GB300.
+
+Workload (one "step"): quest::SignedDistance::computeDistances over 16,777,216
+query points uniform in the 1.2x-expanded box of a level-8 displaced icosphere
+(1,310,720 triangles, 655,362 vertices), all seeded synthetic data
+(axom_gb300.workloads).  The headline ``value`` is the mixed-precision form
+(FP32 outward-rounded traversal, FP64 refine and sign); the plain FP64 form is
+reported beside it, and the BVH build time over the 1,310,720 triangle boxes
+is reported as ``build_ms``.
+
+  python bench.py [--gpus N --steps K --warmup W] [--impl reference]
+
+With N > 1 (launched by torch.distributed.run) every rank holds a replica of
+the mesh and BVH and processes its own 16M points (weak scaling, no
+collective on the data path); ``value`` is the total over ranks divided by
+the slowest rank's time.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+METRIC = "SDF queries/s at 1.3M tris (mixed precision; FP64 path beside it)"
+UNIT = "queries/s"
+LEVEL = 8
+MESH_SEED = 1234
+QUERIES = 1 << 24
+FALLBACK_HBM_GBS = 6800.0
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gsq", choices=["gsq", "reference"])
+    ap.add_argument("--queries", type=int, default=QUERIES)
+    ap.add_argument("--precision", default="mixed", choices=["mixed", "fp64"])
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--cpu-seconds", type=float, default=10.0)
+    return ap.parse_args()
+
+
+def peaks():
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        d = json.loads(p.read_text())
+        return float(d["hbm_gbs"]), "measured"
+    return FALLBACK_HBM_GBS, "fallback"
+
+
+class Clocks:
+    """nvidia-smi samples during the timed region."""
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index: int):
+        self.idx = gpu_index
+        self.proc = None
+        self.f = tempfile.NamedTemporaryFile("w+", suffix=".csv", delete=False)
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.idx}", f"--query-gpu={self.FIELDS}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"], stdout=self.f,
+                                         stderr=subprocess.DEVNULL)
+        except OSError:
+            self.proc = None
+
+    def stop(self):
+        if self.proc is None:
+            return None
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        self.f.flush()
+        rows = [r.split(",") for r in Path(self.f.name).read_text().strip().splitlines() if r.count(",") >= 8]
+        os.unlink(self.f.name)
+        if not rows:
+            return None
+        sm = [float(r[1]) for r in rows if r[1].strip().replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in rows if r[2].strip().replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[k] for r in rows for k in range(4) if "Active" in r[5 + k] and "Not" not in r[5 + k]})
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(rows)}
+
+
+def mesh():
+    from axom_gb300 import workloads as W
+    return W.displaced_icosphere(LEVEL, MESH_SEED)
+
+
+def algorithmic_bytes_per_query(port, v, f, q_sample, threads):
+    """B_q = 32 + 104 N_node + 88 N_leaf with N_node = box tests / 2 and N_leaf
+    = triangle tests, counted by the instrumented oracle on a sample."""
+    h = port.sdf(v[:, 0], v[:, 1], v[:, 2], f)
+    nb, nl = port.sdf_counts(h, q_sample, threads=threads)
+    return 32.0 + 104.0 * nb.mean() / 2.0 + 88.0 * nl.mean(), float(nb.mean()), float(nl.mean())
+
+
+def cpu_baseline(port, v, f, q, seconds, threads):
+    """The oracle port on the host cores, on a bounded stratified sample."""
+    h = port.sdf(v[:, 0], v[:, 1], v[:, 2], f)
+    probe = q[:: max(1, q.shape[0] // 4000)][:4000]
+    t0 = time.perf_counter()
+    port.sdf_eval(h, probe, threads=threads)
+    rate = probe.shape[0] / max(time.perf_counter() - t0, 1e-6)
+    n = int(min(q.shape[0], max(2000, rate * seconds)))
+    sample = q[np.linspace(0, q.shape[0] - 1, n).astype(np.int64)]
+    t0 = time.perf_counter()
+    port.sdf_eval(h, sample, threads=threads)
+    dt = time.perf_counter() - t0
+    return {"value": n / dt, "unit": UNIT, "cores": threads, "kind": "port",
+            "sample": f"{n} stratified points of the {q.shape[0]} (every {q.shape[0] // n}th), "
+                      f"{dt:.1f} s on {threads} host threads"}
+
+
+def dist_setup():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return world, rank, local
+
+
+def run_reference(args, world, rank):
+    """Reference arm: the CPU implementation of the path (oracle port) on all host cores."""
+    if rank != 0:
+        return
+    import oracle
+    from axom_gb300 import workloads as W
+    threads = os.cpu_count() or 1
+    port = oracle.Port()
+    v, f = mesh()
+    q = W.uniform_queries(v, args.queries, 3)
+    h = port.sdf(v[:, 0], v[:, 1], v[:, 2], f)
+    probe = q[:2000]
+    t0 = time.perf_counter()
+    port.sdf_eval(h, probe, threads=threads)
+    rate = probe.shape[0] / (time.perf_counter() - t0)
+    n = int(min(q.shape[0], max(2000, rate * 8.0)))
+    times = []
+    for s in range(args.warmup + args.steps):
+        idx = np.linspace(s, q.shape[0] - 1, n).astype(np.int64)
+        sample = q[idx]
+        t0 = time.perf_counter()
+        port.sdf_eval(h, sample, threads=threads)
+        if s >= args.warmup:
+            times.append(time.perf_counter() - t0)
+    value = n * len(times) / sum(times)
+    line = {"metric": METRIC, "value": value, "unit": UNIT, "impl": "reference", "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000.0 * args.queries / value,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": workload_config(args, f),
+            "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
+                             "sample": f"{n} stratified points of {args.queries} per step, timed on {threads} threads"},
+            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def workload_config(args, f):
+    return {"workload": f"signed distance: displaced icosphere level {LEVEL} ({f.shape[0]} triangles), "
+                        f"{args.queries} uniform points in the 1.2x box per GPU",
+            "mesh_triangles": int(f.shape[0]), "queries_per_gpu": int(args.queries), "precision": args.precision,
+            "l2": "no flush: the 402 MB of query points and outputs per step exceed the 129 MB L2"}
+
+
+def run_gsq(args, world, rank, local):
+    import torch
+    import axom_gb300 as G
+    import oracle
+    from axom_gb300 import workloads as W
+
+    torch.cuda.set_device(local)
+    torch.cuda.init()
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    lib = G.load()
+    v, f = mesh()
+    m = args.queries
+    q_host = W.uniform_queries(v, m, 3 + rank)
+    q_dev = torch.from_numpy(q_host).cuda()
+    prec = G.PRECISION_MIXED if args.precision == "mixed" else G.PRECISION_FP64
+    sd = G.SignedDistance(v, f, precision=prec)
+    out = torch.empty(m, dtype=torch.float64, device="cuda")
+
+    def barrier():
+        if dist is not None:
+            dist.barrier()
+        torch.cuda.synchronize()
+
+    def max_over_ranks(x: float) -> float:
+        if dist is None:
+            return x
+        t = torch.tensor([x], dtype=torch.float64, device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        return float(t.item())
+
+    # BVH build over the 1,310,720 triangle boxes (BVH::initialize).
+    tri = v[f]
+    boxes = torch.from_numpy(np.concatenate([tri.min(1), tri.max(1)], 1)).cuda()
+    bvh = G.BVH()
+    build_ms = []
+    for i in range(args.warmup + args.steps):
+        bvh.initialize(boxes)
+        if i >= args.warmup:
+            build_ms.append(bvh.last_build_ms())
+
+    def run_steps(precision, steps, warmup):
+        sd.set_precision(precision)
+        for _ in range(warmup):
+            sd.compute_distances(q_dev, out=out)
+        barrier()
+        launches0 = lib.gsq_kernel_launches()
+        ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        kms = []
+        ev0.record()
+        for _ in range(steps):
+            sd.compute_distances(q_dev, out=out)
+            kms.append(sd.last_eval_ms())
+        ev1.record()
+        barrier()
+        ms = ev0.elapsed_time(ev1) / steps
+        return max_over_ranks(ms), statistics.mean(kms), lib.gsq_kernel_launches() - launches0
+
+    clocks = Clocks(local)
+    clocks.start()
+    ms, kernel_ms, launches = run_steps(prec, args.steps, args.warmup)
+    clk = clocks.stop()
+    value = world * m / (ms / 1000.0)
+    other = G.PRECISION_FP64 if prec == G.PRECISION_MIXED else None
+    fp64 = None
+    if other is not None:
+        ms64, kms64, _ = run_steps(other, max(1, min(args.steps, 3)), 1)
+        fp64 = {"value": world * m / (ms64 / 1000.0), "ms_per_step": ms64, "kernel_ms": kms64,
+                "speedup_mixed_over_fp64": ms64 / ms}
+        sd.set_precision(prec)
+
+    # End to end through the public API with host buffers: pinned host points in,
+    # pinned host distances out, copies inside the timed region.
+    q_pin = torch.from_numpy(q_host).pin_memory()
+    out_pin = torch.empty(m, dtype=torch.float64).pin_memory()
+    for _ in range(max(1, args.warmup)):
+        sd.compute_distances(q_pin, out=out_pin)
+    barrier()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        sd.compute_distances(q_pin, out=out_pin)
+    barrier()
+    e2e_ms = max_over_ranks((time.perf_counter() - t0) * 1000.0 / args.steps)
+
+    if rank != 0:
+        if dist is not None:
+            dist.destroy_process_group()
+        return
+    hbm, hbm_kind = peaks()
+    threads = os.cpu_count() or 1
+    port = oracle.Port()
+    sample = q_host[np.linspace(0, m - 1, 20000).astype(np.int64)]
+    bq, nb, nl = algorithmic_bytes_per_query(port, v, f, sample, threads)
+    achieved = bq * m / (kernel_ms / 1000.0) / 1e9
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": ms, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f32 traversal + f64 refine" if args.precision == "mixed" else "f64", "data": "synthetic",
+        "config": workload_config(args, f),
+        "fp64": fp64,
+        "build_ms": {"value": statistics.median(build_ms), "boxes": int(f.shape[0]), "runs": len(build_ms)},
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
+                     "traffic": None, "peak_kind": hbm_kind,
+                     "kernel": "k_sdf_mixed" if args.precision == "mixed" else "k_sdf_fp64",
+                     "kernel_ms": kernel_ms,
+                     "algorithmic_bytes_per_query": bq, "box_tests_per_query": nb, "leaf_tests_per_query": nl},
+        "e2e": {"value": world * m / (e2e_ms / 1000.0), "unit": UNIT, "ms_per_step": e2e_ms,
+                "h2d_bytes_per_step": 24 * m, "d2h_bytes_per_step": 8 * m},
+        "gpu_launches": int(launches),
+        "clocks": clk,
+    }
+    if not args.no_cpu_baseline:
+        line["cpu_baseline"] = cpu_baseline(port, v, f, q_host, args.cpu_seconds, threads)
+    print(json.dumps(line), flush=True)
+    if dist is not None:
+        dist.destroy_process_group()
+
+
+def main():
+    args = parse()
+    world, rank, local = dist_setup()
+    if args.impl == "reference":
+        run_reference(args, world, rank)
+    else:
+        run_gsq(args, world, rank, local)
+
+
+if __name__ == "__main__":
+    main()

@@ -22,6 +22,7 @@ import argparse
 import concurrent.futures as cf
 import os
 import re
+import shutil
 import subprocess
 import sys
 from pathlib import Path
@@ -156,6 +157,9 @@ def build(reference: Path, jobs: int) -> Path:
     p = subprocess.run(link, capture_output=True, text=True)
     if p.returncode != 0:
         raise RuntimeError(f"link failed:\n{p.stderr[-4000:]}")
+    # keep only the library: the generated headers/objects are build by-products
+    shutil.rmtree(GEN, ignore_errors=True)
+    shutil.rmtree(OBJ, ignore_errors=True)
     return LIB
 
 
