@@ -48,7 +48,7 @@ class GsqError(RuntimeError):
 
 class SdfOpts(C.Structure):
     _fields_ = [("precision", C.c_int32), ("sort_queries", C.c_int32), ("block_size", C.c_int32),
-                ("reserved", C.c_int32 * 5)]
+                ("audit", C.c_int32), ("reserved", C.c_int32 * 4)]
 
 
 # (name, restype, argtypes) of every entry point declared in include/gsq.h
@@ -82,6 +82,7 @@ SIGNATURES = [
     ("gsq_sdf_mesh_bounds", C.c_int, [_vp, _dp, _dp]),
     ("gsq_sdf_get_bvh", C.c_int, [_vp, C.POINTER(_vp)]),
     ("gsq_sdf_last_eval_ms", C.c_int, [_vp, C.POINTER(C.c_float)]),
+    ("gsq_sdf_mixed_stats", C.c_int, [_vp, _i64p]),
 ]
 
 
@@ -310,6 +311,15 @@ class SignedDistance:
     def set_sort_queries(self, on: bool):
         self._opts.sort_queries = int(on)
         _check(self._lib.gsq_sdf_set_opts(self._h, C.byref(self._opts)))
+
+    def set_audit(self, on: bool):
+        self._opts.audit = int(on)
+        _check(self._lib.gsq_sdf_set_opts(self._h, C.byref(self._opts)))
+
+    def mixed_stats(self) -> dict:
+        c = (C.c_int64 * 4)()
+        _check(self._lib.gsq_sdf_mixed_stats(self._h, c))
+        return {"violations": c[0], "node_fp64": c[1], "leaf_fp64": c[2], "leaf_skipped": c[3]}
 
     def compute_distances(self, points, closest: bool = False, normals: bool = False, out=None):
         """Signed distances of (m, 3) points; optional closest points and unit normals.

@@ -140,7 +140,9 @@ typedef struct gsq_sdf_opts {
   int32_t precision;      /* GSQ_PRECISION_FP64 (default) or GSQ_PRECISION_MIXED */
   int32_t sort_queries;   /* 1: process queries in Morton order (default 1) */
   int32_t block_size;     /* threads per block of the query kernel (0 = default) */
-  int32_t reserved[5];
+  int32_t audit;          /* MIXED only: 1 re-checks every FP32 skip in FP64 and counts
+                             violations and FP64 fallbacks (gsq_sdf_mixed_stats); slow */
+  int32_t reserved[4];
 } gsq_sdf_opts;
 
 /* Fills opts with the defaults. */
@@ -185,6 +187,13 @@ int gsq_sdf_get_bvh(const gsq_sdf* sdf, const gsq_bvh** bvh);
 
 /* Milliseconds of device time of the last gsq_sdf_eval's query kernel. */
 int gsq_sdf_last_eval_ms(const gsq_sdf* sdf, float* ms);
+
+/* Counters of the last audited MIXED evaluation (opts.audit = 1), host int64[4]:
+ *   [0] FP32 skips that the FP64 re-check contradicts (must be 0)
+ *   [1] node visits decided in FP64   [2] leaves refined in FP64
+ *   [3] leaves skipped on the FP32 certificate.
+ * No reference counterpart (the reference has only the FP64 form). */
+int gsq_sdf_mixed_stats(const gsq_sdf* sdf, int64_t* counters);
 
 #ifdef __cplusplus
 }

@@ -1,0 +1,100 @@
+"""GPU: the mixed-precision form (FP32 certified traversal, FP64 refine).
+
+Its distances and closest points must equal the FP64 form (and so the
+reference) bit for bit, with identical signs; the audit mode re-evaluates every
+triangle the FP32 certificate skipped in FP64 and must find no contradiction.
+Tolerances: distances and closest points bit-exact (the stated bar of 1e-12
+relative is met with margin); unit normals 1e-12 absolute."""
+from __future__ import annotations
+
+import numpy as np
+import pytest
+
+import axom_gb300
+from axom_gb300 import workloads as W
+from conftest import assert_bits_equal, golden
+
+pytestmark = pytest.mark.gpu
+
+FIXTURES = ["sdf_uvsphere", "sdf_ico3", "sdf_ico3_open", "sdf_ico3_unsigned", "sdf_quad12"]
+
+
+@pytest.mark.parametrize("name", FIXTURES)
+def test_mixed_matches_golden(gsq, name):
+    g = golden(name)
+    sd = gsq.SignedDistance(g["vertices"], g["cells"], bool(g["watertight"]), bool(g["sign"]),
+                            precision=axom_gb300.PRECISION_MIXED)
+    d, cp, nr = sd.compute_distances(g["queries"], closest=True, normals=True)
+    assert_bits_equal(d, g["dist"], "distance")
+    assert_bits_equal(cp, g["closest"], "closest point")
+    np.testing.assert_allclose(nr, g["normals"], rtol=0, atol=1e-12)
+
+
+def sliver_mesh(seed: int):
+    """A jittered grid surface with many slivers and some zero-area triangles."""
+    rng = np.random.default_rng(seed)
+    n = 40
+    x, y = np.meshgrid(np.linspace(0, 1, n), np.linspace(0, 1, n), indexing="ij")
+    z = 0.05 * np.sin(6 * x) * np.cos(5 * y)
+    v = np.stack([x, y, z], -1).reshape(-1, 3)
+    v[:, :2] += rng.normal(scale=0.004, size=(v.shape[0], 2))
+    i, j = np.meshgrid(np.arange(n - 1), np.arange(n - 1), indexing="ij")
+    a = (i * n + j).ravel()
+    f = np.concatenate([np.stack([a, a + n, a + n + 1], 1), np.stack([a, a + n + 1, a + 1], 1)])
+    # collapse some triangles onto a line (zero area) and squash others into slivers
+    v2 = v.copy()
+    f = f.astype(np.int32)
+    deg = f[::17]
+    v2[deg[:, 2]] = 0.5 * (v2[deg[:, 0]] + v2[deg[:, 1]])
+    return v2, f
+
+
+@pytest.mark.parametrize("case", ["ico5", "ico6", "quad30", "slivers", "open_ico5"])
+def test_mixed_equals_fp64_with_audit(gsq, case):
+    watertight = True
+    if case.startswith("ico"):
+        v, f = W.displaced_icosphere(int(case[3]), 7)
+    elif case == "quad30":
+        v, f = W.quad_sphere(30)
+        v = W.displace(v, 8)
+    elif case == "slivers":
+        v, f = sliver_mesh(3)
+        watertight = False
+    else:
+        v, f = W.displaced_icosphere(5, 9)
+        f = f[np.arange(f.shape[0]) % 5 != 0]
+        watertight = False
+    tri = f[:, :3]
+    q = np.concatenate([W.uniform_queries(v, 30000, 1), W.near_surface_queries(v, tri, 30000, 2),
+                        v[np.arange(0, v.shape[0], 7)]])  # exactly on vertices too
+    sd = gsq.SignedDistance(v, f, is_watertight=watertight, precision=axom_gb300.PRECISION_FP64)
+    d64, cp64, n64 = sd.compute_distances(q, closest=True, normals=True)
+    sd.set_precision(axom_gb300.PRECISION_MIXED)
+    sd.set_audit(True)
+    dm, cpm, nm = sd.compute_distances(q, closest=True, normals=True)
+    st = sd.mixed_stats()
+    assert st["violations"] == 0, st
+    assert_bits_equal(dm, d64, "distance")
+    assert_bits_equal(cpm, cp64, "closest point")
+    np.testing.assert_allclose(nm, n64, rtol=0, atol=1e-12)
+    assert st["leaf_skipped"] > 0
+    sd.set_audit(False)
+    assert_bits_equal(sd.compute_distances(q), d64, "distance without audit")
+
+
+def test_mixed_full_size_near_surface(gsq):
+    """Level-8 mesh (1,310,720 triangles), 16M points: half uniform, half at
+    offsets 1e-9..1e-3 along the normal.  Mixed vs FP64 on the GPU: zero sign
+    mismatches and zero relative error; a sample against the oracle."""
+    import torch
+    v, f = W.displaced_icosphere(8, 1234)
+    m = 1 << 24
+    q = torch.from_numpy(W.mixed_queries(v, f, m, 4)).cuda()
+    sd = gsq.SignedDistance(v, f, precision=axom_gb300.PRECISION_FP64)
+    d64 = sd.compute_distances(q)
+    sd.set_precision(axom_gb300.PRECISION_MIXED)
+    dm = sd.compute_distances(q)
+    assert int((torch.sign(dm) != torch.sign(d64)).sum()) == 0
+    rel = ((dm - d64).abs() / d64.abs().clamp_min(1e-300)).max().item()
+    assert rel <= 1e-12
+    assert torch.equal(dm.view(torch.int64), d64.view(torch.int64))
