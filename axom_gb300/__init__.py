@@ -83,6 +83,7 @@ SIGNATURES = [
     ("gsq_sdf_get_bvh", C.c_int, [_vp, C.POINTER(_vp)]),
     ("gsq_sdf_last_eval_ms", C.c_int, [_vp, C.POINTER(C.c_float)]),
     ("gsq_sdf_mixed_stats", C.c_int, [_vp, _i64p]),
+    ("gsq_sdf_backward", C.c_int, [_vp, _vp, _vp, _vp, C.c_int32, C.c_int32, _vp, _vp, _vp, _vp]),
 ]
 
 
@@ -287,6 +288,7 @@ class SignedDistance:
         c = np.ascontiguousarray(cells, dtype=np.int32) if not _is_torch(cells) \
             else cells.detach().to("cpu").int().numpy()
         npc = c.shape[1] if c.ndim == 2 else 3
+        self.num_vertices = v.shape[0]
         x, y, z = (np.ascontiguousarray(v[:, k]) for k in range(3))
         self._opts = SdfOpts()
         _check(self._lib.gsq_sdf_opts_init(C.byref(self._opts)))
@@ -344,6 +346,19 @@ class SignedDistance:
         _check(self._lib.gsq_sdf_eval(self._h, C.c_void_p(xs.ptr), C.c_void_p(ys.ptr), C.c_void_p(zs.ptr), 1,
                                       xs.n, C.c_void_p(_ptr(out)), None, None, _stream()))
         return out
+
+    def backward(self, points, grad_dist, want_points: bool = True, want_vertices: bool = True):
+        """Adjoint of compute_distances: (dL/dpoints (m,3), dL/dvertices (V,3))."""
+        p = _Arr(points, np.float64, 3)
+        g = _Arr(grad_dist, np.float64)
+        m = p.n
+        gp = p.empty((m, 3), np.float64) if want_points else None
+        gv = p.empty((self.num_vertices, 3), np.float64) if want_vertices else None
+        base = p.ptr
+        _check(self._lib.gsq_sdf_backward(self._h, C.c_void_p(base), C.c_void_p(base + 8), C.c_void_p(base + 16), 3,
+                                          m, C.c_void_p(g.ptr), C.c_void_p(_ptr(gp)) if gp is not None else None,
+                                          C.c_void_p(_ptr(gv)) if gv is not None else None, _stream()))
+        return gp, gv
 
     def compute_distance(self, x: float, y: float, z: float) -> float:
         return float(self.compute_distances(np.array([[x, y, z]]))[0])

@@ -17,7 +17,7 @@
 // signs are bit-identical to the reference.  Queries may be processed in
 // Morton order of the point (results are per point, so order does not change
 // them) for warp coherence and cache reuse.
-#include "gsq_sdf_device.cuh"
+#include "gsq_sdf_handle.cuh"
 
 #include <algorithm>
 #include <cmath>
@@ -155,39 +155,6 @@ using namespace gsq;
 // =============================================================================
 // C ABI: quest::SignedDistance
 // =============================================================================
-struct gsq_sdf
-{
-  int device = 0;
-  gsq_sdf_opts opts;
-  int watertight = 1, sign = 1;
-  int nverts = 0, ncells = 0, npc = 3;
-  double* d_x = nullptr;  // device copies of the mesh (x, y, z, cells in one block)
-  double* d_y = nullptr;
-  double* d_z = nullptr;
-  int* d_cells = nullptr;
-  void* mesh_block = nullptr;
-  double domain[6];
-  gsq_bvh* bvh = nullptr;
-  void* leaves = nullptr;
-  NodeRec32* nodes32 = nullptr;  // mixed form: FP32 node records
-  void* leaves32 = nullptr;      // mixed form: FP32 leaf records
-  float mesh_max = 0.f;          // max |coordinate| of the mesh, rounded up
-  unsigned long long* d_audit = nullptr;
-  long long audit[4] = {0, 0, 0, 0};
-  int* d_err = nullptr;
-  float eval_ms = 0.f;
-};
-
-namespace gsq
-{
-size_t mixed_leaf_bytes(int npc);
-int mixed_prepare(const NodeRec64* nodes64, int n_inner, const void* leaves64, int nleaves, int npc, NodeRec32* nodes32,
-                  void* leaves32, cudaStream_t s);
-int mixed_launch(int npc, const NodeRec64* nodes64, const NodeRec32* nodes32, const void* leaves64,
-                 const void* leaves32, const sdf::QueryPts& qp, int m, const int* order, const sdf::SdfParams& prm,
-                 float mesh_max, double* out, double* out_cp, double* out_n, int* err, unsigned long long* audit,
-                 cudaStream_t s);
-}  // namespace gsq
 
 namespace
 {
@@ -226,6 +193,35 @@ int stage_queries(const double* qx, const double* qy, const double* qz, int stri
   return GSQ_OK;
 }
 }  // namespace
+
+namespace gsq
+{
+int sdf_query_order(const gsq_sdf* h, const QueryPts& qp, int m, uint32_t* keys[2], int* vals[2], const int** order,
+                    cudaStream_t s)
+{
+  *order = nullptr;
+  if(!h->opts.sort_queries || m <= 1) return GSQ_OK;
+  const double* b = bvh_dev(h->bvh)->bounds;
+  double sc[3];
+  for(int d = 0; d < 3; ++d)
+  {
+    const double ext = b[3 + d] - b[d];
+    sc[d] = (ext > 0.0) ? 1.0 / ext : 0.0;
+  }
+  count_launch();
+  k_query_codes<<<grid_for(m, 256), 256, 0, s>>>(qp, m, b[0], b[1], b[2], sc[0], sc[1], sc[2], keys[0]);
+  const int which = radix_sort_pairs(keys, vals, m, 30, true, s, h->d_err);
+  if(which < 0) return which;
+  *order = vals[which];
+  return GSQ_OK;
+}
+
+int stage_query_points(const double* qx, const double* qy, const double* qz, int stride, int m, cudaStream_t s,
+                       InBuf* bufs, QueryPts& qp)
+{
+  return stage_queries(qx, qy, qz, stride, m, s, bufs, qp);
+}
+}  // namespace gsq
 
 extern "C" {
 
@@ -467,3 +463,4 @@ int gsq_sdf_eval(const gsq_sdf* hc, const double* qx, const double* qy, const do
 }
 
 }  // extern "C"
+

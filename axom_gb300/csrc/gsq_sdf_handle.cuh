@@ -1,0 +1,55 @@
+// The signed-distance handle and the interfaces between its translation
+// units (gsq_sdf.cu: set-up and FP64 query; gsq_sdf_mixed.cu: mixed query;
+// gsq_sdf_adjoint.cu: gradients).
+#pragma once
+
+#include "gsq_sdf_device.cuh"
+
+using gsq::NodeRec32;
+using gsq::NodeRec64;
+
+struct gsq_sdf
+{
+  int device = 0;
+  gsq_sdf_opts opts;
+  int watertight = 1, sign = 1;
+  int nverts = 0, ncells = 0, npc = 3;
+  double* d_x = nullptr;  // device copies of the mesh (x, y, z, cells in one block)
+  double* d_y = nullptr;
+  double* d_z = nullptr;
+  int* d_cells = nullptr;
+  void* mesh_block = nullptr;
+  double domain[6];
+  gsq_bvh* bvh = nullptr;
+  void* leaves = nullptr;
+  NodeRec32* nodes32 = nullptr;  // mixed form: FP32 node records
+  void* leaves32 = nullptr;      // mixed form: FP32 leaf records
+  float mesh_max = 0.f;          // max |coordinate| of the mesh, rounded up
+  unsigned long long* d_audit = nullptr;
+  long long audit[4] = {0, 0, 0, 0};
+  int* d_err = nullptr;
+  float eval_ms = 0.f;
+};
+
+namespace gsq
+{
+size_t mixed_leaf_bytes(int npc);
+int mixed_prepare(const NodeRec64* nodes64, int n_inner, const void* leaves64, int nleaves, int npc, NodeRec32* nodes32,
+                  void* leaves32, cudaStream_t s);
+int mixed_launch(int npc, const NodeRec64* nodes64, const NodeRec32* nodes32, const void* leaves64,
+                 const void* leaves32, const sdf::QueryPts& qp, int m, const int* order, const sdf::SdfParams& prm,
+                 float mesh_max, double* out, double* out_cp, double* out_n, int* err, unsigned long long* audit,
+                 cudaStream_t s);
+}  // namespace gsq
+
+namespace gsq
+{
+const BvhDev* bvh_dev(const gsq_bvh* h);
+// Morton order of the queries (sorted by the code of each point in the BVH
+// bounds); keys/vals are 2 x m scratch each.  Returns the order array or null.
+int sdf_query_order(const gsq_sdf* h, const sdf::QueryPts& qp, int m, uint32_t* keys[2], int* vals[2],
+                    const int** order, cudaStream_t s);
+// Stages (possibly host) query coordinates to the device, as gsq_sdf_eval does.
+int stage_query_points(const double* qx, const double* qy, const double* qz, int stride, int m, cudaStream_t s,
+                       InBuf* bufs, sdf::QueryPts& qp);
+}  // namespace gsq

@@ -16,6 +16,8 @@
 // block sets DEVERR_WAIT and continues.
 #include "gsq_internal.cuh"
 
+#include <algorithm>
+
 namespace gsq
 {
 namespace

@@ -188,6 +188,19 @@ int gsq_sdf_get_bvh(const gsq_sdf* sdf, const gsq_bvh** bvh);
 /* Milliseconds of device time of the last gsq_sdf_eval's query kernel. */
 int gsq_sdf_last_eval_ms(const gsq_sdf* sdf, float* ms);
 
+/* Adjoint of gsq_sdf_eval for a loss L(d): given grad_dist = dL/dd (m), returns
+ *   grad_points   m x 3      dL/dq = dL/dd * s * (q - cp) / |q - cp|     (nullable)
+ *   grad_vertices nverts x 3 dL/dV_k = sum over points of -dL/dd * s * b_k * (q - cp)/|q - cp|
+ *                            where b are the barycentric weights of cp on its
+ *                            closest triangle (nullable)
+ * s is the point's sign; at |q - cp| = 0 the contribution is 0.  The vertex
+ * sum is reduced deterministically (stable sort by vertex id, segment sums in
+ * point order), so repeated calls agree bit for bit.  The closest triangles
+ * are those of the forward pass (same traversal).  No counterpart in the
+ * reference, which has no gradient. */
+int gsq_sdf_backward(const gsq_sdf* sdf, const double* qx, const double* qy, const double* qz, int32_t stride,
+                     int32_t m, const double* grad_dist, double* grad_points, double* grad_vertices, void* stream);
+
 /* Counters of the last audited MIXED evaluation (opts.audit = 1), host int64[4]:
  *   [0] FP32 skips that the FP64 re-check contradicts (must be 0)
  *   [1] node visits decided in FP64   [2] leaves refined in FP64

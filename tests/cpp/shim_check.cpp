@@ -1,0 +1,67 @@
+// C++ caller of the gsq.hpp shim, written like the reference's own tests:
+// the 3x3x3 uniform-mesh known answers of spin/tests/spin_bvh.cpp:279-406 and
+// 519-648, and the exact plane of
+// quest/tests/quest_signed_distance_interface.cpp:186-242.
+#include <cmath>
+#include <cstdio>
+#include <set>
+
+#include "gsq.hpp"
+
+static int failures = 0;
+#define EXPECT(c)                                               \
+  do                                                            \
+  {                                                             \
+    if(!(c))                                                    \
+    {                                                           \
+      std::printf("FAILED %s:%d: %s\n", __FILE__, __LINE__, #c); \
+      ++failures;                                               \
+    }                                                           \
+  } while(0)
+
+int main()
+{
+  // 27 cells of a 3x3x3 uniform mesh over [0,3]^3, cell i fastest
+  std::vector<gsq::BoundingBox> cells;
+  for(int k = 0; k < 3; ++k)
+    for(int j = 0; j < 3; ++j)
+      for(int i = 0; i < 3; ++i)
+        cells.push_back({{double(i), double(j), double(k)}, {double(i + 1), double(j + 1), double(k + 1)}});
+  gsq::spin::BVH<3, double> bvh;
+  bvh.setScaleFactor(1.0);
+  EXPECT(bvh.initialize(cells.data(), (int32_t)cells.size()) == gsq::spin::BVH_BUILD_OK);
+  const gsq::BoundingBox b = bvh.getBounds();
+  for(int d = 0; d < 3; ++d) EXPECT(std::fabs(b.min[d]) < 1e-12 && std::fabs(b.max[d] - 3.0) < 1e-12);
+
+  gsq::BoundingBox q[2] = {{{-1, -1, -1}, {2.5, 2.5, 1.5}}, {{-1, -1, -1}, {-0.5, -0.5, -0.5}}};
+  gsq::Candidates c;
+  bvh.findBoundingBoxes(c, 2, q);
+  EXPECT(c.counts[0] == 18 && c.counts[1] == 0);
+  std::set<int> hit(c.candidates.begin() + c.offsets[0], c.candidates.begin() + c.offsets[0] + c.counts[0]);
+  for(int i = 0; i < 18; ++i) EXPECT(hit.count(i) == 1);
+
+  const double up[3] = {1, 1, 1}, down[3] = {-1, -1, -1};
+  gsq::Ray rays[2] = {gsq::Ray({{-1, -1, -1}}, up), gsq::Ray({{-1, -1, -1}}, down)};
+  bvh.findRays(c, 2, rays);
+  EXPECT(c.counts[0] == 15 && c.counts[1] == 0);
+
+  gsq::quest::SurfaceMesh plane;
+  plane.x = {-5, 5, 0, 5, -5};
+  plane.y = {-5, -5, 0, 5, 5};
+  plane.z = {0, 0, 0, 0, 0};
+  plane.cells = {0, 1, 2, 1, 3, 2, 3, 4, 2, 4, 0, 2};
+  for(int precision : {GSQ_PRECISION_FP64, GSQ_PRECISION_MIXED})
+  {
+    gsq::quest::SignedDistance<3> sd(plane, /*isWatertight=*/false, true, precision);
+    for(int k = 0; k < 16; ++k)
+      for(int j = 0; j < 16; ++j)
+        for(int i = 0; i < 16; ++i)
+        {
+          const gsq::Point p {{-4.0 + i * 8.0 / 15, -4.0 + j * 8.0 / 15, -4.0 + k * 8.0 / 15}};
+          const double d = sd.computeDistance(p);
+          EXPECT(std::fabs(d - p.x[2]) <= 4 * 2.220446049250313e-16 * std::fabs(p.x[2]));
+        }
+  }
+  std::printf("%s (%d failures)\n", failures ? "FAIL" : "OK", failures);
+  return failures ? 1 : 0;
+}
