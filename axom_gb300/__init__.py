@@ -84,7 +84,9 @@ SIGNATURES = [
     ("gsq_sdf_last_eval_ms", C.c_int, [_vp, C.POINTER(C.c_float)]),
     ("gsq_sdf_mixed_stats", C.c_int, [_vp, _i64p]),
     ("gsq_sdf_backward", C.c_int, [_vp, _vp, _vp, _vp, C.c_int32, C.c_int32, _vp, _vp, _vp, _vp]),
+    ("gsq_sdf_eval_noalloc", C.c_int, [_vp, _vp, _vp, _vp, C.c_int32, C.c_int32, _vp, _vp]),
 ]
+NOALLOC_MAX_QUERIES = 262144  # GSQ_NOALLOC_MAX_QUERIES in include/gsq.h
 
 
 def load(path: Path | str | None = None) -> C.CDLL:

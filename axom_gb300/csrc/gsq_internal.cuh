@@ -168,6 +168,12 @@ int bvh_build(BvhDev& B, const double* d_boxes, int n, double scale, cudaStream_
 int radix_sort_pairs(uint32_t* keys[2], int* vals[2], int n, int end_bit, bool vals_iota, cudaStream_t s,
                      int* d_err);
 
+// The same sort with a caller-provided workspace of at least
+// radix_sort_work_bytes(n) bytes (no allocation).
+size_t radix_sort_work_bytes(int n);
+int radix_sort_pairs_prealloc(uint32_t* keys[2], int* vals[2], int n, int end_bit, bool vals_iota, void* work,
+                              size_t work_bytes, cudaStream_t s, int* d_err);
+
 // Exclusive scan of m int32 counts into offsets; *d_total (device int64)
 // receives the sum.
 int exclusive_scan(const int* d_in, int* d_out, int m, long long* d_total, cudaStream_t s);

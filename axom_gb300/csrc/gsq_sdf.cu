@@ -22,7 +22,9 @@
 #include <algorithm>
 #include <cmath>
 #include <cstring>
+#include <mutex>
 #include <new>
+#include <string>
 #include <vector>
 
 namespace gsq
@@ -464,3 +466,119 @@ int gsq_sdf_eval(const gsq_sdf* hc, const double* qx, const double* qy, const do
 
 }  // extern "C"
 
+// =============================================================================
+// Allocation-free evaluation
+// =============================================================================
+// Some callers cannot allocate device memory while they evaluate distances:
+// code that owns all device memory through its own pool allocator and forbids
+// other allocations, code whose evaluation runs inside a CUDA stream capture
+// (where cudaMalloc is not allowed), and time-critical loops where the
+// device-wide synchronisation of cudaMalloc/cudaFree is unacceptable.  For them
+// gsq_sdf_eval_noalloc takes the query points and the output in device memory
+// and keeps its only scratch -- the Morton-order sort of the queries -- in the
+// fixed array below, which every GPU that loads this library holds until the
+// process exits.
+namespace
+{
+constexpr int NOALLOC_MAX = GSQ_NOALLOC_MAX_QUERIES;
+// keys[2] + vals[2] (4 arrays of NOALLOC_MAX words) + the sort's histogram and
+// look-back words for NOALLOC_MAX keys (4*256 + 64 tiles * 256 + 32 words).
+constexpr size_t NOALLOC_SORT_WORDS = 4 * 256 + ((NOALLOC_MAX + 4095) / 4096) * 256 + 32;
+constexpr size_t NOALLOC_BYTES = sizeof(uint32_t) * (4 * (size_t)NOALLOC_MAX + NOALLOC_SORT_WORDS);
+static __device__ __align__(256) unsigned char g_noalloc_scratch[NOALLOC_BYTES];
+
+constexpr int NOALLOC_MAX_DEVICES = 64;
+std::mutex g_noalloc_mutex;
+void* g_noalloc_ptr[NOALLOC_MAX_DEVICES] = {};
+
+// Device address of the scratch array on the current device.  In host code
+// the array's name is only a host-side stand-in, so the address comes from
+// cudaGetSymbolAddress, once per device (with that device current).
+int noalloc_scratch(void** out)
+{
+  int dev = 0;
+  GSQ_CUDA_TRY(cudaGetDevice(&dev));
+  if(dev < 0 || dev >= NOALLOC_MAX_DEVICES) return fail(GSQ_ERR_INVALID, "device ordinal out of range");
+  std::lock_guard<std::mutex> lock(g_noalloc_mutex);
+  if(!g_noalloc_ptr[dev])
+  {
+    void* p = nullptr;
+    const cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+    if(e != cudaSuccess) return cuda_fail(e, "cudaGetSymbolAddress(no-alloc scratch)");
+    g_noalloc_ptr[dev] = p;
+  }
+  *out = g_noalloc_ptr[dev];
+  return GSQ_OK;
+}
+}  // namespace
+
+extern "C" {
+
+int gsq_sdf_eval_noalloc(const gsq_sdf* hc, const double* qx, const double* qy, const double* qz, int32_t stride,
+                         int32_t m, double* out, void* stream)
+{
+  gsq_sdf* h = const_cast<gsq_sdf*>(hc);
+  if(!h) return fail(GSQ_ERR_INVALID, "null sdf handle");
+  if(m < 0 || stride < 1) return fail(GSQ_ERR_INVALID, "invalid query count or stride");
+  if(m > NOALLOC_MAX)
+    return fail(GSQ_ERR_INVALID, "gsq_sdf_eval_noalloc: at most GSQ_NOALLOC_MAX_QUERIES (" +
+                                     std::to_string(NOALLOC_MAX) + ") points per call, got " + std::to_string(m));
+  if(m == 0) return GSQ_OK;
+  if(!qx || !qy || !qz || !out) return fail(GSQ_ERR_INVALID, "null query or output array");
+  if(!is_device_ptr(qx) || !is_device_ptr(qy) || !is_device_ptr(qz) || !is_device_ptr(out))
+    return fail(GSQ_ERR_INVALID, "gsq_sdf_eval_noalloc: queries and output must be device memory");
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  void* base = nullptr;
+  int rc = noalloc_scratch(&base);
+  if(rc) return rc;
+  uint32_t* words = static_cast<uint32_t*>(base);
+  uint32_t* keys[2] = {words, words + NOALLOC_MAX};
+  int* vals[2] = {reinterpret_cast<int*>(words + 2 * (size_t)NOALLOC_MAX),
+                  reinterpret_cast<int*>(words + 3 * (size_t)NOALLOC_MAX)};
+  void* sort_work = words + 4 * (size_t)NOALLOC_MAX;
+
+  QueryPts qp {qx, qy, qz, stride};
+  const BvhDev* B = bvh_dev(h->bvh);
+  const int* order = nullptr;
+  if(h->opts.sort_queries && m > 1)
+  {
+    const double* b = B->bounds;
+    double sc[3];
+    for(int d = 0; d < 3; ++d)
+    {
+      const double ext = b[3 + d] - b[d];
+      sc[d] = (ext > 0.0) ? 1.0 / ext : 0.0;
+    }
+    count_launch();
+    k_query_codes<<<grid_for(m, 256), 256, 0, s>>>(qp, m, b[0], b[1], b[2], sc[0], sc[1], sc[2], keys[0]);
+    const int which = radix_sort_pairs_prealloc(keys, vals, m, 30, true, sort_work,
+                                                sizeof(uint32_t) * NOALLOC_SORT_WORDS, s, h->d_err);
+    if(which < 0) return which;
+    order = vals[which];
+  }
+  SdfParams prm;
+  std::memcpy(prm.domain, h->domain, sizeof(prm.domain));
+  prm.watertight = h->watertight;
+  prm.sign = h->sign;
+  if(h->opts.precision == GSQ_PRECISION_MIXED)
+  {
+    rc = mixed_launch(h->npc, B->nodes, h->nodes32, h->leaves, h->leaves32, qp, m, order, prm, h->mesh_max, out,
+                      nullptr, nullptr, h->d_err, nullptr, s);
+    if(rc) return rc;
+  }
+  else
+  {
+    const int threads = 128;
+    count_launch();
+    if(h->npc == 3)
+      k_sdf_fp64<3><<<grid_for(m, threads), threads, 0, s>>>(B->nodes, static_cast<const LeafRec<3>*>(h->leaves), qp,
+                                                            m, order, prm, out, nullptr, nullptr, h->d_err);
+    else
+      k_sdf_fp64<4><<<grid_for(m, threads), threads, 0, s>>>(B->nodes, static_cast<const LeafRec<4>*>(h->leaves), qp,
+                                                            m, order, prm, out, nullptr, nullptr, h->d_err);
+  }
+  GSQ_CUDA_TRY(cudaGetLastError());
+  return check_device_error(h->d_err, s, "gsq_sdf_eval_noalloc");
+}
+
+}  // extern "C"

@@ -300,6 +300,43 @@ int radix_sort_pairs(uint32_t* keys[2], int* vals[2], int n, int end_bit, bool v
   return cur;
 }
 
+size_t radix_sort_work_bytes(int n)
+{
+  const size_t ntiles = ((size_t)std::max(n, 1) + TILE - 1) / TILE;
+  return sizeof(unsigned) * (4 * RADIX + ntiles * RADIX + 32);
+}
+
+int radix_sort_pairs_prealloc(uint32_t* keys[2], int* vals[2], int n, int end_bit, bool vals_iota, void* work,
+                              size_t work_bytes, cudaStream_t s, int* d_err)
+{
+  if(n <= 0) return 0;
+  if(n >= (1 << 30)) return fail(GSQ_ERR_INVALID, "radix sort supports fewer than 2^30 keys");
+  if(!work || work_bytes < radix_sort_work_bytes(n)) return fail(GSQ_ERR_INVALID, "sort workspace too small");
+  const int passes = (end_bit + 7) / 8;
+  const int ntiles = (n + TILE - 1) / TILE;
+  const size_t hist_words = 4 * RADIX;
+  const size_t lb_words = (size_t)ntiles * RADIX;
+  unsigned* hist = static_cast<unsigned*>(work);
+  unsigned* lookback = hist + hist_words;
+  int* tile_counter = reinterpret_cast<int*>(lookback + lb_words);
+  GSQ_CUDA_TRY(cudaMemsetAsync(hist, 0, sizeof(unsigned) * hist_words, s));
+  const int hblocks = (int)std::min<long long>(((long long)n + 1023) / 1024, 1024);
+  k_histogram<<<hblocks, 256, 0, s>>>(keys[0], n, passes, hist);
+  k_histogram_scan<<<1, RADIX, 0, s>>>(hist, passes);
+  count_launch(2 + passes);
+  int cur = 0;
+  for(int p = 0; p < passes; ++p)
+  {
+    GSQ_CUDA_TRY(cudaMemsetAsync(lookback, 0, sizeof(unsigned) * (lb_words + 32), s));
+    k_onesweep<<<ntiles, THREADS, 0, s>>>(keys[cur], vals[cur], (vals_iota && p == 0) ? 1 : 0, keys[cur ^ 1],
+                                          vals[cur ^ 1], n, 8 * p, hist + p * RADIX, lookback, tile_counter,
+                                          d_err);
+    cur ^= 1;
+  }
+  GSQ_CUDA_TRY(cudaGetLastError());
+  return cur;
+}
+
 int exclusive_scan(const int* d_in, int* d_out, int m, long long* d_total, cudaStream_t s)
 {
   if(m <= 0)

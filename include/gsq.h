@@ -177,6 +177,29 @@ int gsq_sdf_set_opts(gsq_sdf* sdf, const gsq_sdf_opts* opts);
 int gsq_sdf_eval(const gsq_sdf* sdf, const double* qx, const double* qy, const double* qz, int32_t stride,
                  int32_t m, double* out, double* closest, double* normals, void* stream);
 
+/* Allocation-free evaluation, for callers that must not allocate device
+ * memory while evaluating: code that owns all device memory through its own
+ * pool, code evaluating inside a CUDA stream capture (where cudaMalloc is not
+ * allowed), and latency-bound loops that cannot afford the device-wide
+ * synchronisation of cudaMalloc/cudaFree.  No counterpart in the reference.
+ *   - qx, qy, qz (with `stride`, as gsq_sdf_eval) and out (m doubles) must be
+ *     device memory; no closest points or normals.
+ *   - m <= GSQ_NOALLOC_MAX_QUERIES, else GSQ_ERR_INVALID and nothing runs.
+ *   - Calls no cudaMalloc/cudaFree or allocating library routine.  The only
+ *     scratch (the Morton-order sort of the points) is one fixed array of
+ *     about 4.3 MB in the library's device image, which every GPU that loads
+ *     the library holds until the process exits.
+ *   - The first call on each device looks the array's device address up once
+ *     (cudaGetSymbolAddress); make that first call before any stream capture.
+ *   - Every call shares that one array: calls whose GPU work overlaps (other
+ *     streams or host threads, on the same device) race and corrupt each
+ *     other's results.  Serialise them.
+ *   - The precision and query-order options of the handle apply; outputs equal
+ *     gsq_sdf_eval's. */
+#define GSQ_NOALLOC_MAX_QUERIES 262144
+int gsq_sdf_eval_noalloc(const gsq_sdf* sdf, const double* qx, const double* qy, const double* qz, int32_t stride,
+                         int32_t m, double* out, void* stream);
+
 /* Replaces signed_distance_get_mesh_bounds (quest/interface/signed_distance.hpp:308):
  * bounding box of the mesh nodes (host lo[3], hi[3]). */
 int gsq_sdf_mesh_bounds(const gsq_sdf* sdf, double* lo, double* hi);
