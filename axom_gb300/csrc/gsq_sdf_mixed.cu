@@ -113,7 +113,7 @@ struct MixedStats
 };
 
 template <int NPC, bool AUDIT>
-__global__ void __launch_bounds__(128) k_sdf_mixed(const NodeRec64* __restrict__ nodes64,
+__global__ void __launch_bounds__(256) k_sdf_mixed(const NodeRec64* __restrict__ nodes64,
                                                    const NodeRec32* __restrict__ nodes32,
                                                    const LeafRec<NPC>* __restrict__ leaves64,
                                                    const LeafRec32<NPC>* __restrict__ leaves32,
@@ -166,9 +166,9 @@ int mixed_prepare(const NodeRec64* nodes64, int n_inner, const void* leaves64, i
 int mixed_launch(int npc, const NodeRec64* nodes64, const NodeRec32* nodes32, const void* leaves64,
                  const void* leaves32, const sdf::QueryPts& qp, int m, const int* order, const sdf::SdfParams& prm,
                  float mesh_max, double* out, double* out_cp, double* out_n, int* err, unsigned long long* audit,
-                 cudaStream_t s)
+                 int block, cudaStream_t s)
 {
-  const int threads = 128;
+  const int threads = (block >= 32 && block <= 256) ? block : 128;
   MixedStats st {audit};
   const int g = grid_for(m, threads);
 #define GSQ_MIXED(NPC, AUD)                                                                                       \
