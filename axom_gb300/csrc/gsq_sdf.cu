@@ -167,6 +167,7 @@ void sdf_release(gsq_sdf* h)
   if(h->nodes32) cudaFree(h->nodes32);
   if(h->leaves32) cudaFree(h->leaves32);
   if(h->d_audit) cudaFree(h->d_audit);
+  if(h->d_work) cudaFree(h->d_work);
   if(h->d_err) cudaFree(h->d_err);
   if(h->bvh) gsq_bvh_destroy(h->bvh);
   delete h;
@@ -315,6 +316,7 @@ int gsq_sdf_create(gsq_sdf** out, const double* x, const double* y, const double
   if(e == cudaSuccess) e = cudaMalloc(&h->nodes32, sizeof(NodeRec32) * std::max(B->n - 1, 1));
   if(e == cudaSuccess) e = cudaMalloc(&h->leaves32, mixed_leaf_bytes(npc) * B->n);
   if(e == cudaSuccess) e = cudaMalloc(&h->d_audit, 4 * sizeof(unsigned long long));
+  if(e == cudaSuccess) e = cudaMalloc(&h->d_work, sizeof(int));
   if(e != cudaSuccess) return bail(cuda_fail(e, "gsq_sdf_create: fp32 records"));
   rc = mixed_prepare(B->nodes, B->n - 1, h->leaves, B->n, npc, h->nodes32, h->leaves32, s);
   if(rc) return bail(rc);
@@ -434,7 +436,7 @@ int gsq_sdf_eval(const gsq_sdf* hc, const double* qx, const double* qy, const do
   {
     rc = mixed_launch(h->npc, B->nodes, h->nodes32, h->leaves, h->leaves32, qp, m, order, prm, h->mesh_max,
                       static_cast<double*>(ob.dev), static_cast<double*>(cb.dev), static_cast<double*>(nb.dev),
-                      h->d_err, audit ? h->d_audit : nullptr, h->opts.block_size, s);
+                      h->d_err, audit ? h->d_audit : nullptr, h->d_work, h->opts.block_size, s);
     if(rc) return rc;
   }
   else
@@ -563,7 +565,7 @@ int gsq_sdf_eval_noalloc(const gsq_sdf* hc, const double* qx, const double* qy, 
   if(h->opts.precision == GSQ_PRECISION_MIXED)
   {
     rc = mixed_launch(h->npc, B->nodes, h->nodes32, h->leaves, h->leaves32, qp, m, order, prm, h->mesh_max, out,
-                      nullptr, nullptr, h->d_err, nullptr, h->opts.block_size, s);
+                      nullptr, nullptr, h->d_err, nullptr, h->d_work, h->opts.block_size, s);
     if(rc) return rc;
   }
   else

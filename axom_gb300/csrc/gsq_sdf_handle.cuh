@@ -26,6 +26,7 @@ struct gsq_sdf
   void* leaves32 = nullptr;      // mixed form: FP32 leaf records
   float mesh_max = 0.f;          // max |coordinate| of the mesh, rounded up
   unsigned long long* d_audit = nullptr;
+  int* d_work = nullptr;          // work-queue counter of the persistent query kernel
   long long audit[4] = {0, 0, 0, 0};
   int* d_err = nullptr;
   float eval_ms = 0.f;
@@ -39,7 +40,7 @@ int mixed_prepare(const NodeRec64* nodes64, int n_inner, const void* leaves64, i
 int mixed_launch(int npc, const NodeRec64* nodes64, const NodeRec32* nodes32, const void* leaves64,
                  const void* leaves32, const sdf::QueryPts& qp, int m, const int* order, const sdf::SdfParams& prm,
                  float mesh_max, double* out, double* out_cp, double* out_n, int* err, unsigned long long* audit,
-                 int block, cudaStream_t s);
+                 int* work, int block, cudaStream_t s);
 }  // namespace gsq
 
 namespace gsq

@@ -112,8 +112,18 @@ struct MixedStats
   unsigned long long* c;  // [0] audit violations [1] node FP64 fallbacks [2] leaf FP64 checks [3] leaf skips
 };
 
+// Persistent warp loop over a work queue of Morton-ordered points.  Each lane
+// runs one point's traversal as a resumable state machine, one FP32 step per
+// iteration.  A lane whose next step needs FP64 (an undecided node visit, a
+// leaf that may change the minimum, or the final sign and outputs) parks;
+// once every live lane of the warp is parked (or BATCH_MIN are), the warp runs
+// the FP64 work converged.  FP64 instructions therefore issue with most lanes
+// active instead of one or two.  Finished lanes take the next point from the
+// queue with one warp-aggregated atomic.
+constexpr int BATCH_MIN = 20;
+
 template <int NPC, bool AUDIT>
-__global__ void __launch_bounds__(256) k_sdf_mixed(const NodeRec64* __restrict__ nodes64,
+__global__ void __launch_bounds__(128) k_sdf_mixed(const NodeRec64* __restrict__ nodes64,
                                                    const NodeRec32* __restrict__ nodes32,
                                                    const LeafRec<NPC>* __restrict__ leaves64,
                                                    const LeafRec32<NPC>* __restrict__ leaves32,
@@ -126,20 +136,181 @@ __global__ void __launch_bounds__(256) k_sdf_mixed(const NodeRec64* __restrict__
                                                    double* __restrict__ out_cp,
                                                    double* __restrict__ out_n,
                                                    int* err,
-                                                   MixedStats stats)
+                                                   MixedStats stats,
+                                                   int* __restrict__ work)
 {
-  const int t = blockIdx.x * blockDim.x + threadIdx.x;
-  if(t >= m) return;
-  const int idx = order ? __ldg(order + t) : t;
-  const double q[3] = {qp.x[(size_t)idx * qp.stride], qp.y[(size_t)idx * qp.stride], qp.z[(size_t)idx * qp.stride]};
+  constexpr unsigned FULL = 0xFFFFFFFFu;
+  constexpr int M_DESCEND = 0, M_LEAF = 1, M_IDLE = 2;
+  constexpr int P_NONE = 0, P_NODE = 1, P_LEAF = 2, P_FINISH = 3;
+  constexpr int ALL = (1 << (NPC - 2)) - 1;
+  const int lane = threadIdx.x & 31;
+  const unsigned lt_mask = (1u << lane) - 1u;
+  const bool computeNormal = prm.sign != 0;
+
+  int idx = 0;
+  double q[3] = {0.0, 0.0, 0.0};
+  QCtx c;
   MinCand mc;
   init_min(mc);
+  int todo[STACK_SIZE];
+  int sp = 0, found = 0, cur = 0;
+  int mode = M_IDLE, pend = P_NONE;
+  int pleaf = 0, pneed = 0;
+  int2 pch = make_int2(0, 0);
+  bool open = true;
   unsigned long long st[4] = {0, 0, 0, 0};
-  if(!mixed_traverse<NPC, AUDIT>(q, mc, nodes64, nodes32, leaves64, leaves32, mesh_max, prm.sign != 0, st))
-    atomicOr(err, DEVERR_STACK);
-  finish_query<NPC>(q, mc, leaves64, prm, idx, out, out_cp, out_n);
+
+  // transitions of the reference traversal (bvh_traverse.hpp:100-133, 140-151)
+  auto pop = [&]() { return (sp >= 0) ? todo[sp--] : BARRIER; };
+  auto apply_visit = [&](bool inL, bool inR, bool swap, int2 ch) {
+    if(!inL && !inR)
+      cur = pop();
+    else
+    {
+      cur = inL ? ch.x : ch.y;
+      int rc = ch.y;
+      if(inL && inR)
+      {
+        if(swap)
+        {
+          const int tmp = cur;
+          cur = rc;
+          rc = tmp;
+        }
+        if(sp + 1 >= STACK_SIZE)
+        {
+          atomicOr(err, DEVERR_STACK);
+          pend = P_FINISH;
+          return;
+        }
+        todo[++sp] = rc;
+      }
+    }
+    if(cur < 0 && !(found < 0))
+    {
+      found = cur;
+      if(cur != BARRIER) cur = pop();
+    }
+  };
+  auto after_leaf = [&]() {
+    found = cur;
+    if(cur < 0 && cur != BARRIER) cur = pop();
+  };
+
+  while(true)
+  {
+    const unsigned want = __ballot_sync(FULL, mode == M_IDLE && open);
+    if(want)
+    {
+      const int leader = __ffs(want) - 1;
+      int base = 0;
+      if(lane == leader) base = atomicAdd(work, __popc(want));
+      base = __shfl_sync(FULL, base, leader);
+      if(mode == M_IDLE && open)
+      {
+        const int t = base + __popc(want & lt_mask);
+        if(t < m)
+        {
+          idx = order ? __ldg(order + t) : t;
+          q[0] = qp.x[(size_t)idx * qp.stride];
+          q[1] = qp.y[(size_t)idx * qp.stride];
+          q[2] = qp.z[(size_t)idx * qp.stride];
+          qctx_init(c, q, mesh_max);
+          init_min(mc);
+          qctx_update(c, mc.minSq);
+          sp = 0;
+          todo[0] = BARRIER;
+          found = 0;
+          cur = 0;
+          mode = M_DESCEND;
+          pend = P_NONE;
+        }
+        else
+          open = false;
+      }
+    }
+    const unsigned live = __ballot_sync(FULL, mode != M_IDLE);
+    if(live == 0) break;
+    const unsigned parked = __ballot_sync(FULL, pend != P_NONE);
+    if(parked && (parked == live || __popc(parked) >= BATCH_MIN))
+    {
+      // converged FP64 work of the parked lanes
+      const int p = pend;
+      pend = P_NONE;
+      if(p == P_NODE)
+      {
+        bool inL, inR, swap;
+        visit_fp64(nodes64, cur, q, mc.minSq, inL, inR, swap);
+        if(AUDIT) ++st[1];
+        apply_visit(inL, inR, swap, pch);
+      }
+      else if(p == P_LEAF)
+      {
+        if(AUDIT) ++st[2];
+        const double before = mc.minSq;
+        leaf_refine<NPC>(leaves64, pleaf, pneed, q, mc, computeNormal);
+        if(mc.minSq != before) qctx_update(c, mc.minSq);
+        after_leaf();
+      }
+      else if(p == P_FINISH)
+      {
+        finish_query<NPC>(q, mc, leaves64, prm, idx, out, out_cp, out_n);
+        mode = M_IDLE;
+      }
+      continue;
+    }
+    if(mode == M_IDLE || pend != P_NONE) continue;
+    // one FP32 step
+    if(mode == M_DESCEND)
+    {
+      if(cur >= 0)
+      {
+        bool inL, inR, swap;
+        int2 ch;
+        if(visit32(nodes32, cur, c, inL, inR, swap, ch))
+          apply_visit(inL, inR, swap, ch);
+        else
+        {
+          pend = P_NODE;
+          pch = ch;
+        }
+      }
+      else
+        mode = M_LEAF;
+    }
+    else
+    {
+      if(found < 0 && found != BARRIER)
+      {
+        const int lp = -found - 1;
+        const int need = leaf_prefilter<NPC>(leaves32, lp, c);
+        if(AUDIT)
+        {
+          if(need == 0) ++st[3];
+          st[0] += leaf_audit<NPC>(leaves64, lp, ALL & ~need, q, mc.minSq);
+        }
+        if(need)
+        {
+          pend = P_LEAF;
+          pleaf = lp;
+          pneed = need;
+        }
+        else
+          after_leaf();
+      }
+      else
+      {
+        found = 0;
+        if(cur == BARRIER)
+          pend = P_FINISH;
+        else
+          mode = M_DESCEND;
+      }
+    }
+  }
   if(AUDIT)
-    for(int k = 0; k < 4; ++k) atomicAdd(stats.c + k, st[k]);
+    for(int k = 0; k < 4; ++k)
+      if(st[k]) atomicAdd(stats.c + k, st[k]);
 }
 
 inline int grid_for(long long n, int threads) { return (int)std::max<long long>(1, (n + threads - 1) / threads); }
@@ -166,15 +337,25 @@ int mixed_prepare(const NodeRec64* nodes64, int n_inner, const void* leaves64, i
 int mixed_launch(int npc, const NodeRec64* nodes64, const NodeRec32* nodes32, const void* leaves64,
                  const void* leaves32, const sdf::QueryPts& qp, int m, const int* order, const sdf::SdfParams& prm,
                  float mesh_max, double* out, double* out_cp, double* out_n, int* err, unsigned long long* audit,
-                 int block, cudaStream_t s)
+                 int* work, int block, cudaStream_t s)
 {
-  const int threads = (block >= 32 && block <= 256) ? block : 128;
+  const int threads = (block >= 32 && block <= 128) ? (block / 32) * 32 : 128;
   MixedStats st {audit};
-  const int g = grid_for(m, threads);
-#define GSQ_MIXED(NPC, AUD)                                                                                       \
-  k_sdf_mixed<NPC, AUD><<<g, threads, 0, s>>>(nodes64, nodes32, static_cast<const LeafRec<NPC>*>(leaves64),      \
-                                              static_cast<const LeafRec32<NPC>*>(leaves32), qp, m, order, prm,    \
-                                              mesh_max, out, out_cp, out_n, err, st)
+  int dev = 0, sms = 0;
+  GSQ_CUDA_TRY(cudaGetDevice(&dev));
+  GSQ_CUDA_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+  GSQ_CUDA_TRY(cudaMemsetAsync(work, 0, sizeof(int), s));
+  int per_sm = 0;
+#define GSQ_MIXED(NPC, AUD)                                                                                         \
+  do                                                                                                                \
+  {                                                                                                                 \
+    GSQ_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_sdf_mixed<NPC, AUD>, threads, 0));       \
+    const long long need = ((long long)m + threads - 1) / threads;                                                  \
+    const int g = (int)std::max<long long>(1, std::min<long long>((long long)sms * std::max(per_sm, 1), need));     \
+    k_sdf_mixed<NPC, AUD><<<g, threads, 0, s>>>(nodes64, nodes32, static_cast<const LeafRec<NPC>*>(leaves64),       \
+                                                static_cast<const LeafRec32<NPC>*>(leaves32), qp, m, order, prm,    \
+                                                mesh_max, out, out_cp, out_n, err, st, work);                       \
+  } while(0)
   if(npc == 3)
   {
     if(audit)

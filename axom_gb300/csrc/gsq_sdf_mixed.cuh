@@ -95,10 +95,159 @@ __device__ __forceinline__ int box_decide(const float* lo, const float* hi, floa
   return 2;
 }
 
-// The certified traversal for one point: the reference traversal with FP32
-// decisions and FP64 fallbacks (see gsq_sdf_mixed.cu).  mc must be
-// initialised.  Returns false on stack overflow.  With AUDIT, stats[0..3]
-// accumulate contradictions, FP64 node decisions, FP64 leaf checks, skips.
+// Per-query constants of the FP32 certificates.
+struct QCtx
+{
+  float qf[3], qlo[3], qhi[3];  // point rounded to nearest, down, up
+  float e2, e3;                 // centroid-order error terms
+  float lip;                    // coordinate-rounding part of the triangle distance error
+  float t_true, t_false;        // box predicate thresholds derived from minSq
+  float thr_leaf;               // sqrt(minSq) + 1e-6, rounded up
+};
+
+__device__ __forceinline__ void qctx_init(QCtx& c, const double* q, float mesh_max)
+{
+  float qabs = 0.f;
+  for(int d = 0; d < 3; ++d)
+  {
+    c.qf[d] = __double2float_rn(q[d]);
+    c.qlo[d] = __double2float_rd(q[d]);
+    c.qhi[d] = __double2float_ru(q[d]);
+    qabs = fmaxf(qabs, fmaxf(fabsf(c.qlo[d]), fabsf(c.qhi[d])));
+  }
+  const float Mq = fmaxf(qabs, mesh_max);
+  // e bounds |(c_f - q_f) - (c - q)| per axis for box centroids c
+  const float e = __fmul_ru(0x1p-20f, Mq);
+  c.e2 = __fmul_ru(3.5f, e);
+  c.e3 = __fmul_ru(3.f * e, e);
+  // the point-triangle distance is 1-Lipschitz in the point and the vertices
+  c.lip = __fmul_ru(0x1p-21f, __fadd_ru(qabs, mesh_max));
+}
+
+__device__ __forceinline__ void qctx_update(QCtx& c, double minSq)
+{
+  c.t_true = __double2float_rd(minSq * (1.0 - 0x1p-40));
+  c.t_false = __double2float_ru(minSq * (1.0 + 0x1p-40));
+  c.thr_leaf = __fadd_ru(__double2float_ru(sqrt(minSq)), 1.0001e-6f);
+}
+
+// One node visit decided in FP32.  Returns false if some decision is not
+// certain (the caller then decides the whole visit in FP64 with visit_fp64).
+__device__ __forceinline__ bool visit32(const NodeRec32* __restrict__ nodes32, int cur, const QCtx& c, bool& inL,
+                                        bool& inR, bool& swap, int2& ch)
+{
+  const float4* r = reinterpret_cast<const float4*>(nodes32 + cur);
+  const float4 a = __ldg(r), b = __ldg(r + 1), cc = __ldg(r + 2);
+  const int4 lk = __ldg(reinterpret_cast<const int4*>(r + 3));
+  ch = make_int2(lk.x, lk.y);
+  const float lo_l[3] = {a.x, a.y, a.z}, hi_l[3] = {a.w, b.x, b.y};
+  const float lo_r[3] = {b.z, b.w, cc.x}, hi_r[3] = {cc.y, cc.z, cc.w};
+  const bool vl = lo_l[0] <= hi_l[0] && lo_l[1] <= hi_l[1] && lo_l[2] <= hi_l[2];
+  const bool vr = lo_r[0] <= hi_r[0] && lo_r[1] <= hi_r[1] && lo_r[2] <= hi_r[2];
+  const int dl = vl ? box_decide(lo_l, hi_l, __int_as_float(lk.z), c.qlo, c.qhi, c.t_true, c.t_false) : 0;
+  const int dr = vr ? box_decide(lo_r, hi_r, __int_as_float(lk.w), c.qlo, c.qhi, c.t_true, c.t_false) : 0;
+  if(dl == 2 || dr == 2) return false;
+  swap = false;
+  if(dl == 1 && dr == 1)
+  {
+    float sl = 0.f, sr = 0.f;
+#pragma unroll
+    for(int d = 0; d < 3; ++d)
+    {
+      const float xl = 0.5f * (lo_l[d] + hi_l[d]) - c.qf[d];
+      const float xr = 0.5f * (lo_r[d] + hi_r[d]) - c.qf[d];
+      sl += xl * xl;
+      sr += xr * xr;
+    }
+    const float bound = c.e2 * (sqrtf(sl) + sqrtf(sr)) + 2.f * c.e3 + 0x1p-20f * (sl + sr);
+    if(sl - sr > bound)
+      swap = true;
+    else if(!(sr - sl > bound))
+      return false;
+  }
+  inL = (dl == 1);
+  inR = (dr == 1);
+  return true;
+}
+
+// FP32 certificate of the leaf action: bit s of the result is set when
+// triangle s may change the running minimum or the pseudo-normal sum and so
+// needs the FP64 checkCandidate.
+template <int NPC>
+__device__ __forceinline__ int leaf_prefilter(const LeafRec32<NPC>* __restrict__ leaves32, int leafpos, const QCtx& c)
+{
+  const float4* r = reinterpret_cast<const float4*>(leaves32 + leafpos);
+  float v[3 * NPC];
+  float ec[2], lt[2];
+  if constexpr(NPC == 3)
+  {
+    const float4 a = __ldg(r), b = __ldg(r + 1), cc = __ldg(r + 2);
+    v[0] = a.x, v[1] = a.y, v[2] = a.z, v[3] = a.w, v[4] = b.x, v[5] = b.y, v[6] = b.z, v[7] = b.w, v[8] = cc.x;
+    ec[0] = cc.y, lt[0] = cc.z;
+  }
+  else
+  {
+    const float4 a = __ldg(r), b = __ldg(r + 1), cc = __ldg(r + 2), d4 = __ldg(r + 3);
+    v[0] = a.x, v[1] = a.y, v[2] = a.z, v[3] = a.w, v[4] = b.x, v[5] = b.y, v[6] = b.z, v[7] = b.w, v[8] = cc.x;
+    v[9] = cc.y, v[10] = cc.z, v[11] = cc.w;
+    ec[0] = d4.x, ec[1] = d4.y, lt[0] = d4.z, lt[1] = d4.w;
+  }
+  int need = 0;
+#pragma unroll
+  for(int s = 0; s < NPC - 2; ++s)
+  {
+    const float* A = v;
+    const float* B = v + 3 * (s + 1);
+    const float* C = v + 3 * (s + 2);
+    const float d2 = dist2_f32(c.qf, A, B, C);
+    const float ap = fmaxf(fabsf(c.qf[0] - A[0]), fmaxf(fabsf(c.qf[1] - A[1]), fabsf(c.qf[2] - A[2])));
+    const float E = __fadd_ru(c.lip, __fmul_ru(ec[s], __fadd_ru(ap, lt[s])));
+    const float lim = __fadd_ru(c.thr_leaf, E);
+    if(!(d2 > __fmul_ru(__fmul_ru(lim, lim), 1.0f + 0x1p-20f))) need |= 1 << s;
+  }
+  return need;
+}
+
+// Audit of a skipped triangle: counts it if the FP64 distance contradicts
+// the certificate (it would lie within sqrt(minSq) + 1e-6).
+template <int NPC>
+__device__ __forceinline__ int leaf_audit(const LeafRec<NPC>* __restrict__ leaves64, int leafpos, int skip_mask,
+                                          const double* q, double minSq)
+{
+  double w[3 * NPC];
+  load_leaf<NPC>(leaves64, leafpos, w);
+  int bad = 0;
+  for(int s = 0; s < NPC - 2; ++s)
+  {
+    if(!(skip_mask & (1 << s))) continue;
+    double cp[3];
+    closest_point(q, w, w + 3 * (s + 1), w + 3 * (s + 2), cp);
+    const double lim64 = sqrt(minSq) + 1e-6;
+    if(sqdist_pp(q, cp) <= lim64 * lim64) ++bad;
+  }
+  return bad;
+}
+
+// FP64 checkCandidate on the triangles of `need`, in the reference's order.
+template <int NPC>
+__device__ __forceinline__ void leaf_refine(const LeafRec<NPC>* __restrict__ leaves64, int leafpos, int need,
+                                            const double* q, MinCand& mc, bool computeNormal)
+{
+  double w[3 * NPC];
+  load_leaf<NPC>(leaves64, leafpos, w);
+#pragma unroll
+  for(int s = 0; s < NPC - 2; ++s)
+  {
+    if(!(need & (1 << s))) continue;
+    const double* T[3] = {w, w + 3 * (s + 1), w + 3 * (s + 2)};
+    check_triangle(q, mc, T, leafpos, s, computeNormal);
+  }
+}
+
+// The certified traversal for one point, one thread at a time (used by the
+// adjoint).  mc must be initialised.  Returns false on stack overflow.  With
+// AUDIT, stats[0..3] accumulate contradictions, FP64 node decisions, FP64
+// leaf checks and skips.
 template <int NPC, bool AUDIT>
 __device__ __forceinline__ bool mixed_traverse(const double* q, MinCand& mc, const NodeRec64* __restrict__ nodes64,
                                                const NodeRec32* __restrict__ nodes32,
@@ -106,153 +255,29 @@ __device__ __forceinline__ bool mixed_traverse(const double* q, MinCand& mc, con
                                                const LeafRec32<NPC>* __restrict__ leaves32, float mesh_max,
                                                bool computeNormal, unsigned long long* stats)
 {
-  float qf[3], qlo[3], qhi[3];
-  float qabs = 0.f;
-  for(int d = 0; d < 3; ++d)
-  {
-    qf[d] = __double2float_rn(q[d]);
-    qlo[d] = __double2float_rd(q[d]);
-    qhi[d] = __double2float_ru(q[d]);
-    qabs = fmaxf(qabs, fmaxf(fabsf(qlo[d]), fabsf(qhi[d])));
-  }
-  const float Mq = fmaxf(qabs, mesh_max);
-  // centroid-order error: e bounds |(c_f - q_f) - (c - q)| per axis
-  const float e = __fmul_ru(0x1p-20f, Mq);
-  const float e2 = __fmul_ru(3.5f, e);
-  const float e3 = __fmul_ru(3.f * e, e);
-  // coordinate-rounding part of the triangle distance error (1-Lipschitz)
-  const float lip = __fmul_ru(0x1p-21f, __fadd_ru(qabs, mesh_max));
-
-  float t_true, t_false, thr_leaf;
-  auto update = [&]() {
-    t_true = __double2float_rd(mc.minSq * (1.0 - 0x1p-40));
-    t_false = __double2float_ru(mc.minSq * (1.0 + 0x1p-40));
-    thr_leaf = __fadd_ru(__double2float_ru(sqrt(mc.minSq)), 1.0001e-6f);
-  };
-  update();
-  unsigned long long n_node64 = 0, n_leaf64 = 0, n_skip = 0, n_bad = 0;
-
+  QCtx c;
+  qctx_init(c, q, mesh_max);
+  qctx_update(c, mc.minSq);
   auto visit = [&](int cur, bool& inL, bool& inR, bool& swap, int2& ch) {
-    const float4* r = reinterpret_cast<const float4*>(nodes32 + cur);
-    const float4 a = __ldg(r), b = __ldg(r + 1), c = __ldg(r + 2);
-    const int4 lk = __ldg(reinterpret_cast<const int4*>(r + 3));
-    ch = make_int2(lk.x, lk.y);
-    const float lo_l[3] = {a.x, a.y, a.z}, hi_l[3] = {a.w, b.x, b.y};
-    const float lo_r[3] = {b.z, b.w, c.x}, hi_r[3] = {c.y, c.z, c.w};
-    const bool vl = lo_l[0] <= hi_l[0] && lo_l[1] <= hi_l[1] && lo_l[2] <= hi_l[2];
-    const bool vr = lo_r[0] <= hi_r[0] && lo_r[1] <= hi_r[1] && lo_r[2] <= hi_r[2];
-    const int dl = vl ? box_decide(lo_l, hi_l, __int_as_float(lk.z), qlo, qhi, t_true, t_false) : 0;
-    const int dr = vr ? box_decide(lo_r, hi_r, __int_as_float(lk.w), qlo, qhi, t_true, t_false) : 0;
-    bool certain = (dl != 2 && dr != 2);
-    swap = false;
-    if(certain && dl == 1 && dr == 1)
-    {
-      float sl = 0.f, sr = 0.f;
-#pragma unroll
-      for(int d = 0; d < 3; ++d)
-      {
-        const float xl = 0.5f * (lo_l[d] + hi_l[d]) - qf[d];
-        const float xr = 0.5f * (lo_r[d] + hi_r[d]) - qf[d];
-        sl += xl * xl;
-        sr += xr * xr;
-      }
-      const float bound = e2 * (sqrtf(sl) + sqrtf(sr)) + 2.f * e3 + 0x1p-20f * (sl + sr);
-      if(sl - sr > bound)
-        swap = true;
-      else if(!(sr - sl > bound))
-        certain = false;
-    }
-    if(certain)
-    {
-      inL = (dl == 1);
-      inR = (dr == 1);
-      return;
-    }
-    if(AUDIT) ++n_node64;
+    if(visit32(nodes32, cur, c, inL, inR, swap, ch)) return;
+    if(AUDIT) ++stats[1];
     visit_fp64(nodes64, cur, q, mc.minSq, inL, inR, swap);
   };
-
   auto leaf = [&](int leafpos) {
-    const float4* r = reinterpret_cast<const float4*>(leaves32 + leafpos);
-    float v[3 * NPC];
-    float ec[2], lt[2];
-    if constexpr(NPC == 3)
+    const int need = leaf_prefilter<NPC>(leaves32, leafpos, c);
+    const int all = (1 << (NPC - 2)) - 1;
+    if(AUDIT)
     {
-      const float4 a = __ldg(r), b = __ldg(r + 1), c = __ldg(r + 2);
-      v[0] = a.x, v[1] = a.y, v[2] = a.z, v[3] = a.w, v[4] = b.x, v[5] = b.y, v[6] = b.z, v[7] = b.w, v[8] = c.x;
-      ec[0] = c.y, lt[0] = c.z;
+      if(need == 0) ++stats[3];
+      stats[0] += leaf_audit<NPC>(leaves64, leafpos, all & ~need, q, mc.minSq);
     }
-    else
-    {
-      const float4 a = __ldg(r), b = __ldg(r + 1), c = __ldg(r + 2), d4 = __ldg(r + 3);
-      v[0] = a.x, v[1] = a.y, v[2] = a.z, v[3] = a.w, v[4] = b.x, v[5] = b.y, v[6] = b.z, v[7] = b.w, v[8] = c.x;
-      v[9] = c.y, v[10] = c.z, v[11] = c.w;
-      ec[0] = d4.x, ec[1] = d4.y, lt[0] = d4.z, lt[1] = d4.w;
-    }
-    bool need[2] = {false, false};
-#pragma unroll
-    for(int s = 0; s < NPC - 2; ++s)
-    {
-      const float* A = v;
-      const float* B = v + 3 * (s + 1);
-      const float* C = v + 3 * (s + 2);
-      const float d2 = dist2_f32(qf, A, B, C);
-      const float ap = fmaxf(fabsf(qf[0] - A[0]), fmaxf(fabsf(qf[1] - A[1]), fabsf(qf[2] - A[2])));
-      const float E = __fadd_ru(lip, __fmul_ru(ec[s], __fadd_ru(ap, lt[s])));
-      const float lim = __fadd_ru(thr_leaf, E);
-      need[s] = !(d2 > __fmul_ru(__fmul_ru(lim, lim), 1.0f + 0x1p-20f));
-    }
-    if(!need[0] && !need[1])
-    {
-      if(AUDIT)
-      {
-        // prove the skip: checkCandidate must be a no-op for every triangle
-        ++n_skip;
-        double w[3 * NPC];
-        load_leaf<NPC>(leaves64, leafpos, w);
-        for(int s = 0; s < NPC - 2; ++s)
-        {
-          double cp[3];
-          closest_point(q, w, w + 3 * (s + 1), w + 3 * (s + 2), cp);
-          const double lim64 = sqrt(mc.minSq) + 1e-6;
-          if(sqdist_pp(q, cp) <= lim64 * lim64) ++n_bad;
-        }
-      }
-      return;
-    }
-    if(AUDIT) ++n_leaf64;
-    double w[3 * NPC];
-    load_leaf<NPC>(leaves64, leafpos, w);
+    if(need == 0) return;
+    if(AUDIT) ++stats[2];
     const double before = mc.minSq;
-#pragma unroll
-    for(int s = 0; s < NPC - 2; ++s)
-    {
-      if(!need[s])
-      {
-        if(AUDIT)
-        {
-          double cp[3];
-          closest_point(q, w, w + 3 * (s + 1), w + 3 * (s + 2), cp);
-          const double lim64 = sqrt(mc.minSq) + 1e-6;
-          if(sqdist_pp(q, cp) <= lim64 * lim64) ++n_bad;
-        }
-        continue;
-      }
-      const double* T[3] = {w, w + 3 * (s + 1), w + 3 * (s + 2)};
-      check_triangle(q, mc, T, leafpos, s, computeNormal);
-    }
-    if(mc.minSq != before) update();
+    leaf_refine<NPC>(leaves64, leafpos, need, q, mc, computeNormal);
+    if(mc.minSq != before) qctx_update(c, mc.minSq);
   };
-
-  const bool ok = traverse_point(visit, leaf);
-  if(AUDIT)
-  {
-    stats[0] += n_bad;
-    stats[1] += n_node64;
-    stats[2] += n_leaf64;
-    stats[3] += n_skip;
-  }
-  return ok;
+  return traverse_point(visit, leaf);
 }
 }  // namespace sdf
 }  // namespace gsq
