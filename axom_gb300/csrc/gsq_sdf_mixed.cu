@@ -114,13 +114,19 @@ struct MixedStats
 
 // Persistent warp loop over a work queue of Morton-ordered points.  Each lane
 // runs one point's traversal as a resumable state machine, one FP32 step per
-// iteration.  A lane whose next step needs FP64 (an undecided node visit, a
-// leaf that may change the minimum, or the final sign and outputs) parks;
-// once every live lane of the warp is parked (or BATCH_MIN are), the warp runs
-// the FP64 work converged.  FP64 instructions therefore issue with most lanes
-// active instead of one or two.  Finished lanes take the next point from the
-// queue with one warp-aggregated atomic.
+// iteration.  Leaves that the FP32 certificate cannot skip are queued (up to
+// QCAP per lane) instead of being refined at once: until they are refined the
+// exact running minimum is only known to lie in an interval (the resolved
+// minimum and certified bounds of the queued candidates' FP64 distances), and
+// every later decision is certified against the whole interval.  A lane parks
+// when its queue is full, when a node decision is uncertain, or at its end;
+// once every live lane of the warp is parked (or BATCH_MIN are) the warp
+// replays the parked lanes' queues in order in FP64, converged.  The FP64 state
+// therefore evolves through exactly the reference's checkCandidate calls on
+// exactly the reference's candidates.  Finished lanes take the next point from
+// the queue of Morton-ordered points with one warp-aggregated atomic.
 constexpr int BATCH_MIN = 20;
+constexpr int QCAP = 16;
 
 template <int NPC, bool AUDIT>
 __global__ void __launch_bounds__(128) k_sdf_mixed(const NodeRec64* __restrict__ nodes64,
@@ -141,7 +147,7 @@ __global__ void __launch_bounds__(128) k_sdf_mixed(const NodeRec64* __restrict__
 {
   constexpr unsigned FULL = 0xFFFFFFFFu;
   constexpr int M_DESCEND = 0, M_LEAF = 1, M_IDLE = 2;
-  constexpr int P_NONE = 0, P_NODE = 1, P_LEAF = 2, P_FINISH = 3;
+  constexpr int P_NONE = 0, P_NODE = 1, P_FLUSH = 2, P_FINISH = 3;
   constexpr int ALL = (1 << (NPC - 2)) - 1;
   const int lane = threadIdx.x & 31;
   const unsigned lt_mask = (1u << lane) - 1u;
@@ -153,13 +159,18 @@ __global__ void __launch_bounds__(128) k_sdf_mixed(const NodeRec64* __restrict__
   MinCand mc;
   init_min(mc);
   int todo[STACK_SIZE];
+  int pq[QCAP];  // queued leaves: leafpos * 4 + mask of triangles to refine
+  int np = 0;
+  float plo = INFINITY, phi = INFINITY;  // bounds on the queued candidates' best FP64 distance^2
   int sp = 0, found = 0, cur = 0;
   int mode = M_IDLE, pend = P_NONE;
-  int pleaf = 0, pneed = 0;
   int2 pch = make_int2(0, 0);
   bool open = true;
   unsigned long long st[4] = {0, 0, 0, 0};
 
+  auto set_thresholds = [&]() {
+    qctx_set(c, fmin(mc.minSq, (double)plo), fmin(mc.minSq, (double)phi));
+  };
   // transitions of the reference traversal (bvh_traverse.hpp:100-133, 140-151)
   auto pop = [&]() { return (sp >= 0) ? todo[sp--] : BARRIER; };
   auto apply_visit = [&](bool inL, bool inR, bool swap, int2 ch) {
@@ -217,6 +228,8 @@ __global__ void __launch_bounds__(128) k_sdf_mixed(const NodeRec64* __restrict__
           q[2] = qp.z[(size_t)idx * qp.stride];
           qctx_init(c, q, mesh_max);
           init_min(mc);
+          np = 0;
+          plo = phi = INFINITY;
           qctx_update(c, mc.minSq);
           sp = 0;
           todo[0] = BARRIER;
@@ -234,23 +247,24 @@ __global__ void __launch_bounds__(128) k_sdf_mixed(const NodeRec64* __restrict__
     const unsigned parked = __ballot_sync(FULL, pend != P_NONE);
     if(parked && (parked == live || __popc(parked) >= BATCH_MIN))
     {
-      // converged FP64 work of the parked lanes
+      // converged FP64 work of the parked lanes: replay the queue in order
       const int p = pend;
       pend = P_NONE;
+      if(p != P_NONE)
+      {
+        for(int j = 0; j < np; ++j)
+          leaf_refine<NPC>(leaves64, pq[j] >> 2, pq[j] & 3, q, mc, computeNormal);
+        if(AUDIT) st[2] += np;
+        np = 0;
+        plo = phi = INFINITY;
+        qctx_update(c, mc.minSq);
+      }
       if(p == P_NODE)
       {
         bool inL, inR, swap;
         visit_fp64(nodes64, cur, q, mc.minSq, inL, inR, swap);
         if(AUDIT) ++st[1];
         apply_visit(inL, inR, swap, pch);
-      }
-      else if(p == P_LEAF)
-      {
-        if(AUDIT) ++st[2];
-        const double before = mc.minSq;
-        leaf_refine<NPC>(leaves64, pleaf, pneed, q, mc, computeNormal);
-        if(mc.minSq != before) qctx_update(c, mc.minSq);
-        after_leaf();
       }
       else if(p == P_FINISH)
       {
@@ -283,20 +297,22 @@ __global__ void __launch_bounds__(128) k_sdf_mixed(const NodeRec64* __restrict__
       if(found < 0 && found != BARRIER)
       {
         const int lp = -found - 1;
-        const int need = leaf_prefilter<NPC>(leaves32, lp, c);
+        float lo2, hi2;
+        const int need = leaf_prefilter_bounds<NPC>(leaves32, lp, c, lo2, hi2);
         if(AUDIT)
         {
           if(need == 0) ++st[3];
-          st[0] += leaf_audit<NPC>(leaves64, lp, ALL & ~need, q, mc.minSq);
+          st[0] += leaf_audit<NPC>(leaves64, lp, ALL & ~need, q, fmin(mc.minSq, (double)phi));
         }
         if(need)
         {
-          pend = P_LEAF;
-          pleaf = lp;
-          pneed = need;
+          pq[np++] = lp * 4 + need;
+          plo = fminf(plo, lo2);
+          phi = fminf(phi, hi2);
+          set_thresholds();
+          if(np == QCAP) pend = P_FLUSH;
         }
-        else
-          after_leaf();
+        after_leaf();
       }
       else
       {

@@ -75,34 +75,15 @@ __device__ __forceinline__ float dist2_f32(const float* P, const float* A, const
   return x * x + y * y + z * z;
 }
 
-// 0: certainly false, 1: certainly true, 2: undecided.
-__device__ __forceinline__ int box_decide(const float* lo, const float* hi, float slack, const float* qlo,
-                                          const float* qhi, float t_true, float t_false)
-{
-  float L = 0.f, H = 0.f;
-#pragma unroll
-  for(int d = 0; d < 3; ++d)
-  {
-    const float gl = fmaxf(fmaxf(__fsub_rd(lo[d], qhi[d]), __fsub_rd(qlo[d], hi[d])), 0.f);
-    const float gh = fmaxf(fmaxf(__fadd_ru(__fsub_ru(lo[d], qlo[d]), slack), __fadd_ru(__fsub_ru(qhi[d], hi[d]), slack)),
-                           0.f);
-    L = __fadd_rd(L, __fmul_rd(gl, gl));
-    H = __fadd_ru(H, __fmul_ru(gh, gh));
-  }
-  if(!(slack < INFINITY)) H = INFINITY;
-  if(L > t_false) return 0;
-  if(H <= t_true) return 1;
-  return 2;
-}
-
 // Per-query constants of the FP32 certificates.
 struct QCtx
 {
-  float qf[3], qlo[3], qhi[3];  // point rounded to nearest, down, up
-  float e2, e3;                 // centroid-order error terms
-  float lip;                    // coordinate-rounding part of the triangle distance error
-  float t_true, t_false;        // box predicate thresholds derived from minSq
-  float thr_leaf;               // sqrt(minSq) + 1e-6, rounded up
+  float qf[3];           // the point rounded to nearest
+  float eq;              // bound on the point's rounding plus subtraction rounding (per axis)
+  float ec;              // the same for the centroid-order test
+  float lip;             // coordinate-rounding part of the triangle distance error
+  float t_true, t_false; // box predicate thresholds from the interval holding minSq
+  float thr_leaf;        // sqrt(upper end of that interval) + 1e-6, rounded up
 };
 
 __device__ __forceinline__ void qctx_init(QCtx& c, const double* q, float mesh_max)
@@ -111,28 +92,48 @@ __device__ __forceinline__ void qctx_init(QCtx& c, const double* q, float mesh_m
   for(int d = 0; d < 3; ++d)
   {
     c.qf[d] = __double2float_rn(q[d]);
-    c.qlo[d] = __double2float_rd(q[d]);
-    c.qhi[d] = __double2float_ru(q[d]);
-    qabs = fmaxf(qabs, fmaxf(fabsf(c.qlo[d]), fabsf(c.qhi[d])));
+    qabs = fmaxf(qabs, fabsf(c.qf[d]));
   }
   const float Mq = fmaxf(qabs, mesh_max);
-  // e bounds |(c_f - q_f) - (c - q)| per axis for box centroids c
-  const float e = __fmul_ru(0x1p-20f, Mq);
-  c.e2 = __fmul_ru(3.5f, e);
-  c.e3 = __fmul_ru(3.f * e, e);
+  c.eq = __fmul_ru(0x1p-21f, Mq);
+  c.ec = __fmul_ru(0x1p-18f, Mq);
   // the point-triangle distance is 1-Lipschitz in the point and the vertices
   c.lip = __fmul_ru(0x1p-21f, __fadd_ru(qabs, mesh_max));
 }
 
-__device__ __forceinline__ void qctx_update(QCtx& c, double minSq)
+// Thresholds for an exact FP64 minimum known to lie in [lo, hi].
+__device__ __forceinline__ void qctx_set(QCtx& c, double lo, double hi)
 {
-  c.t_true = __double2float_rd(minSq * (1.0 - 0x1p-40));
-  c.t_false = __double2float_ru(minSq * (1.0 + 0x1p-40));
-  c.thr_leaf = __fadd_ru(__double2float_ru(sqrt(minSq)), 1.0001e-6f);
+  c.t_true = __double2float_rd(lo * (1.0 - 0x1p-40));
+  c.t_false = __double2float_ru(hi * (1.0 + 0x1p-40));
+  c.thr_leaf = __fadd_ru(__double2float_ru(sqrt(hi)), 1.0001e-6f);
+}
+
+__device__ __forceinline__ void qctx_update(QCtx& c, double minSq) { qctx_set(c, minSq, minSq); }
+
+// squared_distance(p, box) <= minSq decided in FP32 (SD:576-578).  g is the
+// per-axis gap to the outward-rounded box in round-to-nearest; each differs
+// from the exact gap to the FP64 box by at most del = slack + eq, so
+// |sum g^2 - d^2| <= 2 del sum g + 3 del^2 + (FP32 rounding of the sum).
+// 0: certainly false, 1: certainly true, 2: undecided.
+__device__ __forceinline__ int box_decide(const float* lo, const float* hi, float slack, const QCtx& c)
+{
+  const float del = slack + c.eq;
+  const float g0 = fmaxf(fmaxf(lo[0] - c.qf[0], c.qf[0] - hi[0]), 0.f);
+  const float g1 = fmaxf(fmaxf(lo[1] - c.qf[1], c.qf[1] - hi[1]), 0.f);
+  const float g2 = fmaxf(fmaxf(lo[2] - c.qf[2], c.qf[2] - hi[2]), 0.f);
+  const float d2 = g0 * g0 + g1 * g1 + g2 * g2;
+  const float err = 2.02f * del * (g0 + g1 + g2) + 3.03f * del * del + 0x1p-21f * d2;
+  if(!(err < INFINITY)) return 2;
+  if(__fsub_rd(d2, err) > c.t_false) return 0;
+  if(__fadd_ru(d2, err) <= c.t_true) return 1;
+  return 2;
 }
 
 // One node visit decided in FP32.  Returns false if some decision is not
 // certain (the caller then decides the whole visit in FP64 with visit_fp64).
+// The child order compares 4(sl - sr) = sum_d a_d b_d with a = 2(c_L - c_R)
+// and b = 2(c_L + c_R - 2p); each factor is within dc of its exact value.
 __device__ __forceinline__ bool visit32(const NodeRec32* __restrict__ nodes32, int cur, const QCtx& c, bool& inL,
                                         bool& inR, bool& swap, int2& ch)
 {
@@ -142,27 +143,32 @@ __device__ __forceinline__ bool visit32(const NodeRec32* __restrict__ nodes32, i
   ch = make_int2(lk.x, lk.y);
   const float lo_l[3] = {a.x, a.y, a.z}, hi_l[3] = {a.w, b.x, b.y};
   const float lo_r[3] = {b.z, b.w, cc.x}, hi_r[3] = {cc.y, cc.z, cc.w};
+  const float sl_ = __int_as_float(lk.z), sr_ = __int_as_float(lk.w);
   const bool vl = lo_l[0] <= hi_l[0] && lo_l[1] <= hi_l[1] && lo_l[2] <= hi_l[2];
   const bool vr = lo_r[0] <= hi_r[0] && lo_r[1] <= hi_r[1] && lo_r[2] <= hi_r[2];
-  const int dl = vl ? box_decide(lo_l, hi_l, __int_as_float(lk.z), c.qlo, c.qhi, c.t_true, c.t_false) : 0;
-  const int dr = vr ? box_decide(lo_r, hi_r, __int_as_float(lk.w), c.qlo, c.qhi, c.t_true, c.t_false) : 0;
+  const int dl = vl ? box_decide(lo_l, hi_l, sl_, c) : 0;
+  const int dr = vr ? box_decide(lo_r, hi_r, sr_, c) : 0;
   if(dl == 2 || dr == 2) return false;
   swap = false;
   if(dl == 1 && dr == 1)
   {
-    float sl = 0.f, sr = 0.f;
+    float dot = 0.f, mag = 0.f, prod = 0.f;
 #pragma unroll
     for(int d = 0; d < 3; ++d)
     {
-      const float xl = 0.5f * (lo_l[d] + hi_l[d]) - c.qf[d];
-      const float xr = 0.5f * (lo_r[d] + hi_r[d]) - c.qf[d];
-      sl += xl * xl;
-      sr += xr * xr;
+      const float sL = lo_l[d] + hi_l[d], sR = lo_r[d] + hi_r[d];
+      const float av = sL - sR;
+      const float bv = (sL + sR) - 4.f * c.qf[d];
+      dot += av * bv;
+      mag += fabsf(av) + fabsf(bv);
+      prod += fabsf(av * bv);
     }
-    const float bound = c.e2 * (sqrtf(sl) + sqrtf(sr)) + 2.f * c.e3 + 0x1p-20f * (sl + sr);
-    if(sl - sr > bound)
+    const float dc = 2.f * (sl_ + sr_) + c.ec;
+    const float bound = 1.01f * (dc * mag + 3.f * dc * dc + 0x1p-20f * prod);
+    if(!(bound < INFINITY)) return false;
+    if(dot > bound)
       swap = true;
-    else if(!(sr - sl > bound))
+    else if(!(dot < -bound))
       return false;
   }
   inL = (dl == 1);
@@ -204,6 +210,60 @@ __device__ __forceinline__ int leaf_prefilter(const LeafRec32<NPC>* __restrict__
     const float E = __fadd_ru(c.lip, __fmul_ru(ec[s], __fadd_ru(ap, lt[s])));
     const float lim = __fadd_ru(c.thr_leaf, E);
     if(!(d2 > __fmul_ru(__fmul_ru(lim, lim), 1.0f + 0x1p-20f))) need |= 1 << s;
+  }
+  return need;
+}
+
+// leaf_prefilter that also bounds, for the triangles it keeps, the squared
+// distance the FP64 checkCandidate will compute: [lo2, hi2] holds the minimum
+// over the kept triangles.  The upper end adds the FP64 routine's own
+// departure from the exact distance: its fuzzy region tests (EPS 1e-12 on dot
+// products, closest_point.hpp:181-282) move the point by at most
+// 1e-12 / (shortest edge) <= 1e-12 kappa / (longest edge), doubled here.
+template <int NPC>
+__device__ __forceinline__ int leaf_prefilter_bounds(const LeafRec32<NPC>* __restrict__ leaves32, int leafpos,
+                                                     const QCtx& c, float& lo2, float& hi2)
+{
+  const float4* r = reinterpret_cast<const float4*>(leaves32 + leafpos);
+  float v[3 * NPC];
+  float ec[2], lt[2];
+  if constexpr(NPC == 3)
+  {
+    const float4 a = __ldg(r), b = __ldg(r + 1), cc = __ldg(r + 2);
+    v[0] = a.x, v[1] = a.y, v[2] = a.z, v[3] = a.w, v[4] = b.x, v[5] = b.y, v[6] = b.z, v[7] = b.w, v[8] = cc.x;
+    ec[0] = cc.y, lt[0] = cc.z;
+  }
+  else
+  {
+    const float4 a = __ldg(r), b = __ldg(r + 1), cc = __ldg(r + 2), d4 = __ldg(r + 3);
+    v[0] = a.x, v[1] = a.y, v[2] = a.z, v[3] = a.w, v[4] = b.x, v[5] = b.y, v[6] = b.z, v[7] = b.w, v[8] = cc.x;
+    v[9] = cc.y, v[10] = cc.z, v[11] = cc.w;
+    ec[0] = d4.x, ec[1] = d4.y, lt[0] = d4.z, lt[1] = d4.w;
+  }
+  int need = 0;
+  lo2 = INFINITY;
+  hi2 = INFINITY;
+#pragma unroll
+  for(int s = 0; s < NPC - 2; ++s)
+  {
+    const float* A = v;
+    const float* B = v + 3 * (s + 1);
+    const float* C = v + 3 * (s + 2);
+    const float d2 = dist2_f32(c.qf, A, B, C);
+    const float ap = fmaxf(fabsf(c.qf[0] - A[0]), fmaxf(fabsf(c.qf[1] - A[1]), fabsf(c.qf[2] - A[2])));
+    const float E = __fadd_ru(c.lip, __fmul_ru(ec[s], __fadd_ru(ap, lt[s])));
+    const float lim = __fadd_ru(c.thr_leaf, E);
+    if(!(d2 > __fmul_ru(__fmul_ru(lim, lim), 1.0f + 0x1p-20f)))
+    {
+      need |= 1 << s;
+      const float kappa = ec[s] * (1.f / (256.f * 0x1p-24f));
+      const float fz = __fdiv_ru(__fmul_ru(2e-12f, kappa), lt[s]);
+      const float dl = fmaxf(__fsub_rd(__fsqrt_rd(__fmul_rd(d2, 1.f - 0x1p-20f)), E), 0.f);
+      const float dh = __fadd_ru(__fadd_ru(__fsqrt_ru(__fmul_ru(d2, 1.f + 0x1p-20f)), E), fz);
+      const float l2 = __fmul_rd(dl, dl), h2 = __fmul_ru(dh, dh);
+      lo2 = (d2 == d2) ? fminf(lo2, l2) : 0.f;
+      hi2 = (d2 == d2 && h2 == h2) ? fminf(hi2, h2) : hi2;
+    }
   }
   return need;
 }
