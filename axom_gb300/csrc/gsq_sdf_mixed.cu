@@ -160,6 +160,7 @@ __global__ void __launch_bounds__(128) k_sdf_mixed(const NodeRec64* __restrict__
   init_min(mc);
   int todo[STACK_SIZE];
   int pq[QCAP];  // queued leaves: leafpos * 4 + mask of triangles to refine
+  float aq[AUDIT ? 2 * QCAP : 1];  // audit only: the bounds each queued entry was given
   int np = 0;
   float plo = INFINITY, phi = INFINITY;  // bounds on the queued candidates' best FP64 distance^2
   int sp = 0, found = 0, cur = 0;
@@ -252,6 +253,24 @@ __global__ void __launch_bounds__(128) k_sdf_mixed(const NodeRec64* __restrict__
       pend = P_NONE;
       if(p != P_NONE)
       {
+        if(AUDIT)
+        {
+          // every queued bound must hold for the FP64 distance it stood for
+          for(int j = 0; j < np; ++j)
+          {
+            double w[3 * NPC];
+            load_leaf<NPC>(leaves64, pq[j] >> 2, w);
+            double best = DBL_MAX;
+            for(int t2 = 0; t2 < NPC - 2; ++t2)
+              if((pq[j] & 3) & (1 << t2))
+              {
+                double cp[3];
+                closest_point(q, w, w + 3 * (t2 + 1), w + 3 * (t2 + 2), cp);
+                best = fmin(best, sqdist_pp(q, cp));
+              }
+            if(!(best >= (double)aq[2 * j] && best <= (double)aq[2 * j + 1])) ++st[0];
+          }
+        }
         for(int j = 0; j < np; ++j)
           leaf_refine<NPC>(leaves64, pq[j] >> 2, pq[j] & 3, q, mc, computeNormal);
         if(AUDIT) st[2] += np;
@@ -306,6 +325,11 @@ __global__ void __launch_bounds__(128) k_sdf_mixed(const NodeRec64* __restrict__
         }
         if(need)
         {
+          if(AUDIT)
+          {
+            aq[2 * np] = lo2;
+            aq[2 * np + 1] = hi2;
+          }
           pq[np++] = lp * 4 + need;
           plo = fminf(plo, lo2);
           phi = fminf(phi, hi2);

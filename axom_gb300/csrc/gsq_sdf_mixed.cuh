@@ -216,10 +216,14 @@ __device__ __forceinline__ int leaf_prefilter(const LeafRec32<NPC>* __restrict__
 
 // leaf_prefilter that also bounds, for the triangles it keeps, the squared
 // distance the FP64 checkCandidate will compute: [lo2, hi2] holds the minimum
-// over the kept triangles.  The upper end adds the FP64 routine's own
-// departure from the exact distance: its fuzzy region tests (EPS 1e-12 on dot
-// products, closest_point.hpp:181-282) move the point by at most
-// 1e-12 / (shortest edge) <= 1e-12 kappa / (longest edge), doubled here.
+// over the kept triangles.  The FP64 point always lies on the triangle, so the
+// lower end needs only the FP32 error.  The upper end adds the FP64 routine's
+// own departure from the exact closest point: its fuzzy region tests
+// (closest_point.hpp:181-282) use a fixed EPS = 1e-12 on dot products
+// (length^2), which moves the point by at most 1e-12 / (shortest edge)
+// <= 1e-12 kappa / L, and on the products vc, vb, va (length^4), which moves
+// it by at most 1e-12 / (edge |n|) <= 1e-12 kappa^2 / L^3 (for the small
+// triangles of fine meshes this is ~1e-6, far above rounding); both doubled.
 template <int NPC>
 __device__ __forceinline__ int leaf_prefilter_bounds(const LeafRec32<NPC>* __restrict__ leaves32, int leafpos,
                                                      const QCtx& c, float& lo2, float& hi2)
@@ -257,7 +261,8 @@ __device__ __forceinline__ int leaf_prefilter_bounds(const LeafRec32<NPC>* __res
     {
       need |= 1 << s;
       const float kappa = ec[s] * (1.f / (256.f * 0x1p-24f));
-      const float fz = __fdiv_ru(__fmul_ru(2e-12f, kappa), lt[s]);
+      const float kl = __fdiv_ru(kappa, lt[s]);
+      const float fz = __fmul_ru(2e-12f, __fadd_ru(kl, __fdiv_ru(__fmul_ru(kl, kl), lt[s])));
       const float dl = fmaxf(__fsub_rd(__fsqrt_rd(__fmul_rd(d2, 1.f - 0x1p-20f)), E), 0.f);
       const float dh = __fadd_ru(__fadd_ru(__fsqrt_ru(__fmul_ru(d2, 1.f + 0x1p-20f)), E), fz);
       const float l2 = __fmul_rd(dl, dl), h2 = __fmul_ru(dh, dh);

@@ -82,6 +82,24 @@ def test_mixed_equals_fp64_with_audit(gsq, case):
     assert_bits_equal(sd.compute_distances(q), d64, "distance without audit")
 
 
+def test_mixed_audit_fine_mesh(gsq):
+    """Level-8 triangles are small (edges ~0.008), where the reference's fixed
+    fuzzy EPS moves its closest point the most; the audit checks every skip
+    and every queued candidate's distance bounds."""
+    import torch
+    v, f = W.displaced_icosphere(8, 1234)
+    q = torch.from_numpy(W.mixed_queries(v, f, 1 << 20, 9)).cuda()
+    sd = gsq.SignedDistance(v, f, precision=axom_gb300.PRECISION_FP64)
+    d64, cp64, _ = sd.compute_distances(q, closest=True)
+    sd.set_precision(axom_gb300.PRECISION_MIXED)
+    sd.set_audit(True)
+    dm, cpm, _ = sd.compute_distances(q, closest=True)
+    st = sd.mixed_stats()
+    assert st["violations"] == 0, st
+    assert torch.equal(dm.view(torch.int64), d64.view(torch.int64))
+    assert torch.equal(cpm.view(torch.int64), cp64.view(torch.int64))
+
+
 def test_mixed_full_size_near_surface(gsq):
     """Level-8 mesh (1,310,720 triangles), 16M points: half uniform, half at
     offsets 1e-9..1e-3 along the normal.  Mixed vs FP64 on the GPU: zero sign
