@@ -48,7 +48,7 @@ class GsqError(RuntimeError):
 
 class SdfOpts(C.Structure):
     _fields_ = [("precision", C.c_int32), ("sort_queries", C.c_int32), ("block_size", C.c_int32),
-                ("audit", C.c_int32), ("reserved", C.c_int32 * 4)]
+                ("audit", C.c_int32), ("queue_depth", C.c_int32), ("reserved", C.c_int32 * 3)]
 
 
 # (name, restype, argtypes) of every entry point declared in include/gsq.h

@@ -436,7 +436,7 @@ int gsq_sdf_eval(const gsq_sdf* hc, const double* qx, const double* qy, const do
   {
     rc = mixed_launch(h->npc, B->nodes, h->nodes32, h->leaves, h->leaves32, qp, m, order, prm, h->mesh_max,
                       static_cast<double*>(ob.dev), static_cast<double*>(cb.dev), static_cast<double*>(nb.dev),
-                      h->d_err, audit ? h->d_audit : nullptr, h->d_work, h->opts.block_size, s);
+                      h->d_err, audit ? h->d_audit : nullptr, h->d_work, h->opts.block_size, h->opts.queue_depth, s);
     if(rc) return rc;
   }
   else
@@ -565,7 +565,7 @@ int gsq_sdf_eval_noalloc(const gsq_sdf* hc, const double* qx, const double* qy, 
   if(h->opts.precision == GSQ_PRECISION_MIXED)
   {
     rc = mixed_launch(h->npc, B->nodes, h->nodes32, h->leaves, h->leaves32, qp, m, order, prm, h->mesh_max, out,
-                      nullptr, nullptr, h->d_err, nullptr, h->d_work, h->opts.block_size, s);
+                      nullptr, nullptr, h->d_err, nullptr, h->d_work, h->opts.block_size, h->opts.queue_depth, s);
     if(rc) return rc;
   }
   else

@@ -40,7 +40,7 @@ int mixed_prepare(const NodeRec64* nodes64, int n_inner, const void* leaves64, i
 int mixed_launch(int npc, const NodeRec64* nodes64, const NodeRec32* nodes32, const void* leaves64,
                  const void* leaves32, const sdf::QueryPts& qp, int m, const int* order, const sdf::SdfParams& prm,
                  float mesh_max, double* out, double* out_cp, double* out_n, int* err, unsigned long long* audit,
-                 int* work, int block, cudaStream_t s);
+                 int* work, int block, int depth, cudaStream_t s);
 }  // namespace gsq
 
 namespace gsq

@@ -126,9 +126,8 @@ struct MixedStats
 // exactly the reference's candidates.  Finished lanes take the next point from
 // the queue of Morton-ordered points with one warp-aggregated atomic.
 constexpr int BATCH_MIN = 20;
-constexpr int QCAP = 16;
 
-template <int NPC, bool AUDIT>
+template <int NPC, bool AUDIT, int QCAP>
 __global__ void __launch_bounds__(128) k_sdf_mixed(const NodeRec64* __restrict__ nodes64,
                                                    const NodeRec32* __restrict__ nodes32,
                                                    const LeafRec<NPC>* __restrict__ leaves64,
@@ -377,8 +376,9 @@ int mixed_prepare(const NodeRec64* nodes64, int n_inner, const void* leaves64, i
 int mixed_launch(int npc, const NodeRec64* nodes64, const NodeRec32* nodes32, const void* leaves64,
                  const void* leaves32, const sdf::QueryPts& qp, int m, const int* order, const sdf::SdfParams& prm,
                  float mesh_max, double* out, double* out_cp, double* out_n, int* err, unsigned long long* audit,
-                 int* work, int block, cudaStream_t s)
+                 int* work, int block, int depth, cudaStream_t s)
 {
+  if(depth != 4 && depth != 16) depth = 1;
   const int threads = (block >= 32 && block <= 128) ? (block / 32) * 32 : 128;
   MixedStats st {audit};
   int dev = 0, sms = 0;
@@ -386,15 +386,25 @@ int mixed_launch(int npc, const NodeRec64* nodes64, const NodeRec32* nodes32, co
   GSQ_CUDA_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
   GSQ_CUDA_TRY(cudaMemsetAsync(work, 0, sizeof(int), s));
   int per_sm = 0;
-#define GSQ_MIXED(NPC, AUD)                                                                                         \
+#define GSQ_MIXED3(NPC, AUD, QC)                                                                                    \
   do                                                                                                                \
   {                                                                                                                 \
-    GSQ_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_sdf_mixed<NPC, AUD>, threads, 0));       \
+    GSQ_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_sdf_mixed<NPC, AUD, QC>, threads, 0));   \
     const long long need = ((long long)m + threads - 1) / threads;                                                  \
     const int g = (int)std::max<long long>(1, std::min<long long>((long long)sms * std::max(per_sm, 1), need));     \
-    k_sdf_mixed<NPC, AUD><<<g, threads, 0, s>>>(nodes64, nodes32, static_cast<const LeafRec<NPC>*>(leaves64),       \
-                                                static_cast<const LeafRec32<NPC>*>(leaves32), qp, m, order, prm,    \
-                                                mesh_max, out, out_cp, out_n, err, st, work);                       \
+    k_sdf_mixed<NPC, AUD, QC><<<g, threads, 0, s>>>(nodes64, nodes32, static_cast<const LeafRec<NPC>*>(leaves64),   \
+                                                    static_cast<const LeafRec32<NPC>*>(leaves32), qp, m, order,     \
+                                                    prm, mesh_max, out, out_cp, out_n, err, st, work);              \
+  } while(0)
+#define GSQ_MIXED(NPC, AUD)        \
+  do                               \
+  {                                \
+    if(depth == 16)                \
+      GSQ_MIXED3(NPC, AUD, 16);    \
+    else if(depth == 4)            \
+      GSQ_MIXED3(NPC, AUD, 4);     \
+    else                           \
+      GSQ_MIXED3(NPC, AUD, 1);     \
   } while(0)
   if(npc == 3)
   {
@@ -410,6 +420,7 @@ int mixed_launch(int npc, const NodeRec64* nodes64, const NodeRec32* nodes32, co
     else
       GSQ_MIXED(4, false);
   }
+#undef GSQ_MIXED3
 #undef GSQ_MIXED
   count_launch();
   GSQ_CUDA_TRY(cudaGetLastError());

@@ -142,7 +142,9 @@ typedef struct gsq_sdf_opts {
   int32_t block_size;     /* threads per block of the query kernel (0 = default) */
   int32_t audit;          /* MIXED only: 1 re-checks every FP32 skip in FP64 and counts
                              violations and FP64 fallbacks (gsq_sdf_mixed_stats); slow */
-  int32_t reserved[4];
+  int32_t queue_depth;    /* MIXED only: FP64 refinements a lane queues before they run
+                             (1, 4 or 16; 0 = default 1) */
+  int32_t reserved[3];
 } gsq_sdf_opts;
 
 /* Fills opts with the defaults. */
