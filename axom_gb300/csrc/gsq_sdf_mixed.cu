@@ -162,14 +162,18 @@ __global__ void __launch_bounds__(128) k_sdf_mixed(const NodeRec64* __restrict__
   float aq[AUDIT ? 2 * QCAP : 1];  // audit only: the bounds each queued entry was given
   int np = 0;
   float plo = INFINITY, phi = INFINITY;  // bounds on the queued candidates' best FP64 distance^2
+  float mlo = INFINITY, mhi = INFINITY;  // the resolved minSq rounded down and up
   int sp = 0, found = 0, cur = 0;
   int mode = M_IDLE, pend = P_NONE;
   int2 pch = make_int2(0, 0);
   bool open = true;
   unsigned long long st[4] = {0, 0, 0, 0};
 
-  auto set_thresholds = [&]() {
-    qctx_set(c, fmin(mc.minSq, (double)plo), fmin(mc.minSq, (double)phi));
+  auto set_thresholds = [&]() { qctx_set32(c, fminf(mlo, plo), fminf(mhi, phi)); };
+  auto resolved = [&]() {
+    qctx_update(c, mc.minSq);
+    mlo = __double2float_rd(mc.minSq);
+    mhi = __double2float_ru(mc.minSq);
   };
   // transitions of the reference traversal (bvh_traverse.hpp:100-133, 140-151)
   auto pop = [&]() { return (sp >= 0) ? todo[sp--] : BARRIER; };
@@ -230,7 +234,7 @@ __global__ void __launch_bounds__(128) k_sdf_mixed(const NodeRec64* __restrict__
           init_min(mc);
           np = 0;
           plo = phi = INFINITY;
-          qctx_update(c, mc.minSq);
+          resolved();
           sp = 0;
           todo[0] = BARRIER;
           found = 0;
@@ -275,7 +279,7 @@ __global__ void __launch_bounds__(128) k_sdf_mixed(const NodeRec64* __restrict__
         if(AUDIT) st[2] += np;
         np = 0;
         plo = phi = INFINITY;
-        qctx_update(c, mc.minSq);
+        resolved();
       }
       if(p == P_NODE)
       {
@@ -321,6 +325,7 @@ __global__ void __launch_bounds__(128) k_sdf_mixed(const NodeRec64* __restrict__
         {
           if(need == 0) ++st[3];
           st[0] += leaf_audit<NPC>(leaves64, lp, ALL & ~need, q, fmin(mc.minSq, (double)phi));
+          if(np > 0 && !(mc.minSq >= (double)mlo && mc.minSq <= (double)mhi)) ++st[0];
         }
         if(need)
         {
@@ -330,10 +335,14 @@ __global__ void __launch_bounds__(128) k_sdf_mixed(const NodeRec64* __restrict__
             aq[2 * np + 1] = hi2;
           }
           pq[np++] = lp * 4 + need;
-          plo = fminf(plo, lo2);
-          phi = fminf(phi, hi2);
-          set_thresholds();
-          if(np == QCAP) pend = P_FLUSH;
+          if(np == QCAP)
+            pend = P_FLUSH;
+          else
+          {
+            plo = fminf(plo, lo2);
+            phi = fminf(phi, hi2);
+            set_thresholds();
+          }
         }
         after_leaf();
       }

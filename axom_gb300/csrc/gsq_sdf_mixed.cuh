@@ -79,7 +79,7 @@ __device__ __forceinline__ float dist2_f32(const float* P, const float* A, const
 struct QCtx
 {
   float qf[3];           // the point rounded to nearest
-  float eq;              // bound on the point's rounding plus subtraction rounding (per axis)
+  float eq;              // bound on the point's rounding (per axis)
   float ec;              // the same for the centroid-order test
   float lip;             // coordinate-rounding part of the triangle distance error
   float t_true, t_false; // box predicate thresholds from the interval holding minSq
@@ -95,7 +95,9 @@ __device__ __forceinline__ void qctx_init(QCtx& c, const double* q, float mesh_m
     qabs = fmaxf(qabs, fabsf(c.qf[d]));
   }
   const float Mq = fmaxf(qabs, mesh_max);
-  c.eq = __fmul_ru(0x1p-21f, Mq);
+  // |qf - q| <= 2^-24 |q|; the subtraction in a gap is exact or contributes at
+  // most 2^-24 of the gap, which the relative term of box_decide covers
+  c.eq = __fmul_ru(0x1p-23f, qabs);
   c.ec = __fmul_ru(0x1p-18f, Mq);
   // the point-triangle distance is 1-Lipschitz in the point and the vertices
   c.lip = __fmul_ru(0x1p-21f, __fadd_ru(qabs, mesh_max));
@@ -111,10 +113,19 @@ __device__ __forceinline__ void qctx_set(QCtx& c, double lo, double hi)
 
 __device__ __forceinline__ void qctx_update(QCtx& c, double minSq) { qctx_set(c, minSq, minSq); }
 
+// The same from FP32 bounds lo <= minSq <= hi (no FP64 work).
+__device__ __forceinline__ void qctx_set32(QCtx& c, float lo, float hi)
+{
+  c.t_true = __fmul_rd(lo, 1.f - 0x1p-22f);
+  c.t_false = __fmul_ru(hi, 1.f + 0x1p-22f);
+  c.thr_leaf = __fadd_ru(__fsqrt_ru(hi), 1.0001e-6f);
+}
+
 // squared_distance(p, box) <= minSq decided in FP32 (SD:576-578).  g is the
 // per-axis gap to the outward-rounded box in round-to-nearest; each differs
-// from the exact gap to the FP64 box by at most del = slack + eq, so
-// |sum g^2 - d^2| <= 2 del sum g + 3 del^2 + (FP32 rounding of the sum).
+// from the exact gap to the FP64 box by at most del = slack + eq plus 2^-24 g,
+// so |sum g^2 - d^2| <= 2 del sum g + 3 del^2 + 2^-21 sum g^2 (which also
+// covers the FP32 rounding of the sum).
 // 0: certainly false, 1: certainly true, 2: undecided.
 __device__ __forceinline__ int box_decide(const float* lo, const float* hi, float slack, const QCtx& c)
 {
