@@ -121,20 +121,26 @@ __device__ __forceinline__ void qctx_set32(QCtx& c, float lo, float hi)
   c.thr_leaf = __fadd_ru(__fsqrt_ru(hi), 1.0001e-6f);
 }
 
-// squared_distance(p, box) <= minSq decided in FP32 (SD:576-578).  g is the
-// per-axis gap to the outward-rounded box in round-to-nearest; each differs
-// from the exact gap to the FP64 box by at most del = slack + eq plus 2^-24 g,
-// so |sum g^2 - d^2| <= 2 del sum g + 3 del^2 + 2^-21 sum g^2 (which also
-// covers the FP32 rounding of the sum).
-// 0: certainly false, 1: certainly true, 2: undecided.
+// squared_distance(p, box) <= minSq decided in FP32 (SD:576-578).  s is the
+// per-axis signed gap to the outward-rounded box in round-to-nearest (> 0
+// outside); it differs from the exact signed gap to the FP64 box by at most
+// del = slack + eq plus 2^-24 |s|.  An axis with s < -del (plus that term) has
+// an exact gap of 0 and contributes no error; the others contribute
+// 2 del g + del^2, and 2^-21 sum g^2 covers the relative terms and the FP32
+// rounding of the sum.  0: certainly false, 1: certainly true, 2: undecided.
 __device__ __forceinline__ int box_decide(const float* lo, const float* hi, float slack, const QCtx& c)
 {
   const float del = slack + c.eq;
-  const float g0 = fmaxf(fmaxf(lo[0] - c.qf[0], c.qf[0] - hi[0]), 0.f);
-  const float g1 = fmaxf(fmaxf(lo[1] - c.qf[1], c.qf[1] - hi[1]), 0.f);
-  const float g2 = fmaxf(fmaxf(lo[2] - c.qf[2], c.qf[2] - hi[2]), 0.f);
+  const float s0 = fmaxf(lo[0] - c.qf[0], c.qf[0] - hi[0]);
+  const float s1 = fmaxf(lo[1] - c.qf[1], c.qf[1] - hi[1]);
+  const float s2 = fmaxf(lo[2] - c.qf[2], c.qf[2] - hi[2]);
+  const float g0 = fmaxf(s0, 0.f), g1 = fmaxf(s1, 0.f), g2 = fmaxf(s2, 0.f);
+  const float lim = -1.01f * del;
+  const float n0 = (s0 * 0.999f < lim) ? 0.f : 1.f;
+  const float n1 = (s1 * 0.999f < lim) ? 0.f : 1.f;
+  const float n2 = (s2 * 0.999f < lim) ? 0.f : 1.f;
   const float d2 = g0 * g0 + g1 * g1 + g2 * g2;
-  const float err = 2.02f * del * (g0 + g1 + g2) + 3.03f * del * del + 0x1p-21f * d2;
+  const float err = 2.02f * del * (g0 + g1 + g2) + 1.01f * del * del * (n0 + n1 + n2) + 0x1p-21f * d2;
   if(!(err < INFINITY)) return 2;
   if(__fsub_rd(d2, err) > c.t_false) return 0;
   if(__fadd_ru(d2, err) <= c.t_true) return 1;
