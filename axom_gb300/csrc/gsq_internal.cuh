@@ -11,7 +11,7 @@
 #include <cstdint>
 #include <string>
 
-#include "../../include/gsq.h"
+#include "gsq.h"
 
 namespace gsq
 {

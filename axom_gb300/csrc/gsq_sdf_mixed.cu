@@ -158,6 +158,7 @@ __global__ void __launch_bounds__(128) k_sdf_mixed(const NodeRec64* __restrict__
   MinCand mc;
   init_min(mc);
   int todo[STACK_SIZE];
+  todo[0] = BARRIER;
   int pq[QCAP];  // queued leaves: leafpos * 4 + mask of triangles to refine
   float aq[AUDIT ? 2 * QCAP : 1];  // audit only: the bounds each queued entry was given
   int np = 0;
