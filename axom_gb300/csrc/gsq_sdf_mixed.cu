@@ -128,7 +128,7 @@ struct MixedStats
 constexpr int BATCH_MIN = 20;
 
 template <int NPC, bool AUDIT, int QCAP>
-__global__ void __launch_bounds__(128) k_sdf_mixed(const NodeRec64* __restrict__ nodes64,
+__global__ void __launch_bounds__(128, 5) k_sdf_mixed(const NodeRec64* __restrict__ nodes64,
                                                    const NodeRec32* __restrict__ nodes32,
                                                    const LeafRec<NPC>* __restrict__ leaves64,
                                                    const LeafRec32<NPC>* __restrict__ leaves32,
@@ -164,17 +164,33 @@ __global__ void __launch_bounds__(128) k_sdf_mixed(const NodeRec64* __restrict__
   int np = 0;
   float plo = INFINITY, phi = INFINITY;  // bounds on the queued candidates' best FP64 distance^2
   float mlo = INFINITY, mhi = INFINITY;  // the resolved minSq rounded down and up
+  float qcp[3 * QCAP], qrad[QCAP];        // queued candidates' FP32 closest points and their error radii
+  float mpf[3] = {0.f, 0.f, 0.f};         // the resolved closest point in FP32
+  bool mvalid = false;                    // the resolved state holds a closest point
+  bool reset = false;                     // a queued candidate superseded the resolved state
   int sp = 0, found = 0, cur = 0;
   int mode = M_IDLE, pend = P_NONE;
   int2 pch = make_int2(0, 0);
   bool open = true;
   unsigned long long st[4] = {0, 0, 0, 0};
 
-  auto set_thresholds = [&]() { qctx_set32(c, fminf(mlo, plo), fminf(mhi, phi)); };
+  auto set_thresholds = [&]() {
+    qctx_set32(c, fminf(reset ? INFINITY : mlo, plo), fminf(reset ? INFINITY : mhi, phi));
+  };
   auto resolved = [&]() {
     qctx_update(c, mc.minSq);
     mlo = __double2float_rd(mc.minSq);
     mhi = __double2float_ru(mc.minSq);
+    mvalid = mc.minSq < DBL_MAX;
+    for(int d = 0; d < 3; ++d) mpf[d] = (float)mc.mp[d];
+    reset = false;
+  };
+  // |a - b| > 1e-6 + r for certain: the candidate's point is farther than the
+  // pseudo-normal window from b, so checkCandidate clears (SD:684-690)
+  auto far = [&](const float* a, const float* b, float r) {
+    const float dx = a[0] - b[0], dy = a[1] - b[1], dz = a[2] - b[2];
+    const float lim = __fadd_ru(1.0001e-6f, r);
+    return __fmul_rd(0.999f, dx * dx + dy * dy + dz * dz) > __fmul_ru(lim, lim);
   };
   // transitions of the reference traversal (bvh_traverse.hpp:100-133, 140-151)
   auto pop = [&]() { return (sp >= 0) ? todo[sp--] : BARRIER; };
@@ -257,6 +273,7 @@ __global__ void __launch_bounds__(128) k_sdf_mixed(const NodeRec64* __restrict__
       pend = P_NONE;
       if(p != P_NONE)
       {
+        if(reset) init_min(mc);
         if(AUDIT)
         {
           // every queued bound must hold for the FP64 distance it stood for
@@ -320,8 +337,8 @@ __global__ void __launch_bounds__(128) k_sdf_mixed(const NodeRec64* __restrict__
       if(found < 0 && found != BARRIER)
       {
         const int lp = -found - 1;
-        float lo2, hi2;
-        const int need = leaf_prefilter_bounds<NPC>(leaves32, lp, c, lo2, hi2);
+        float lo2, hi2, cpf[3], rad;
+        const int need = leaf_prefilter_bounds<NPC>(leaves32, lp, c, lo2, hi2, cpf, rad);
         if(AUDIT)
         {
           if(need == 0) ++st[3];
@@ -330,11 +347,43 @@ __global__ void __launch_bounds__(128) k_sdf_mixed(const NodeRec64* __restrict__
         }
         if(need)
         {
+          // A candidate that certainly lowers the minimum below everything
+          // before it and certainly clears (its point is far from every earlier
+          // closest point) leaves the state of checkCandidate independent of
+          // all earlier candidates: they are dropped unevaluated.
+          if(need == 1 || need == 2)
+          {
+            bool sup = hi2 < fminf(reset ? INFINITY : mlo, plo);
+            if(sup && !reset && mvalid) sup = far(cpf, mpf, __fadd_ru(rad, __fmul_ru(0x1p-22f, mesh_max)));
+            for(int j = 0; sup && j < np; ++j) sup = far(cpf, qcp + 3 * j, __fadd_ru(rad, qrad[j]));
+            if(sup)
+            {
+              if(AUDIT)
+              {
+                MinCand s1 = mc, s2;
+                if(reset) init_min(s1);
+                for(int j = 0; j < np; ++j) leaf_refine<NPC>(leaves64, pq[j] >> 2, pq[j] & 3, q, s1, computeNormal);
+                leaf_refine<NPC>(leaves64, lp, need, q, s1, computeNormal);
+                init_min(s2);
+                leaf_refine<NPC>(leaves64, lp, need, q, s2, computeNormal);
+                const bool same = s1.minSq == s2.minSq && s1.type == s2.type && s1.leaf == s2.leaf &&
+                                  s1.sub == s2.sub && s1.mp[0] == s2.mp[0] && s1.mp[1] == s2.mp[1] &&
+                                  s1.mp[2] == s2.mp[2] && s1.sn[0] == s2.sn[0] && s1.sn[1] == s2.sn[1] &&
+                                  s1.sn[2] == s2.sn[2];
+                if(!same) ++st[0];
+              }
+              np = 0;
+              plo = phi = INFINITY;
+              reset = true;
+            }
+          }
           if(AUDIT)
           {
             aq[2 * np] = lo2;
             aq[2 * np + 1] = hi2;
           }
+          for(int d = 0; d < 3; ++d) qcp[3 * np + d] = cpf[d];
+          qrad[np] = rad;
           pq[np++] = lp * 4 + need;
           if(np == QCAP)
             pend = P_FLUSH;
@@ -388,7 +437,7 @@ int mixed_launch(int npc, const NodeRec64* nodes64, const NodeRec32* nodes32, co
                  float mesh_max, double* out, double* out_cp, double* out_n, int* err, unsigned long long* audit,
                  int* work, int block, int depth, cudaStream_t s)
 {
-  if(depth != 4 && depth != 16) depth = 1;
+  if(depth != 1 && depth != 16) depth = 4;
   const int threads = (block >= 32 && block <= 128) ? (block / 32) * 32 : 128;
   MixedStats st {audit};
   int dev = 0, sms = 0;

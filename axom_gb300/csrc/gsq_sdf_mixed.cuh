@@ -31,48 +31,50 @@ static_assert(sizeof(LeafRec32<4>) == 64, "fp32 quad leaf is 64 bytes");
 namespace sdf
 {
 // Squared point-triangle distance in FP32 by Voronoi regions (Ericson,
-// Real-Time Collision Detection 5.1.5), measured from P.
-__device__ __forceinline__ float dist2_f32(const float* P, const float* A, const float* B, const float* C)
+// Real-Time Collision Detection 5.1.5), measured from P.  off (optional)
+// receives P - cp, the offset from the closest point.
+__device__ __forceinline__ float dist2_f32(const float* P, const float* A, const float* B, const float* C,
+                                          float* off = nullptr)
 {
+  auto ret = [&](float x, float y, float z) {
+    if(off) off[0] = x, off[1] = y, off[2] = z;
+    return x * x + y * y + z * z;
+  };
   const float ab0 = B[0] - A[0], ab1 = B[1] - A[1], ab2 = B[2] - A[2];
   const float ac0 = C[0] - A[0], ac1 = C[1] - A[1], ac2 = C[2] - A[2];
   const float ap0 = P[0] - A[0], ap1 = P[1] - A[1], ap2 = P[2] - A[2];
   const float d1 = ab0 * ap0 + ab1 * ap1 + ab2 * ap2;
   const float d2 = ac0 * ap0 + ac1 * ap1 + ac2 * ap2;
-  if(d1 <= 0.f && d2 <= 0.f) return ap0 * ap0 + ap1 * ap1 + ap2 * ap2;
+  if(d1 <= 0.f && d2 <= 0.f) return ret(ap0, ap1, ap2);
   const float bp0 = P[0] - B[0], bp1 = P[1] - B[1], bp2 = P[2] - B[2];
   const float d3 = ab0 * bp0 + ab1 * bp1 + ab2 * bp2;
   const float d4 = ac0 * bp0 + ac1 * bp1 + ac2 * bp2;
-  if(d3 >= 0.f && d4 <= d3) return bp0 * bp0 + bp1 * bp1 + bp2 * bp2;
+  if(d3 >= 0.f && d4 <= d3) return ret(bp0, bp1, bp2);
   const float vc = d1 * d4 - d3 * d2;
   if(vc <= 0.f && d1 >= 0.f && d3 <= 0.f)
   {
     const float v = d1 / (d1 - d3);
-    const float x = ap0 - v * ab0, y = ap1 - v * ab1, z = ap2 - v * ab2;
-    return x * x + y * y + z * z;
+    return ret(ap0 - v * ab0, ap1 - v * ab1, ap2 - v * ab2);
   }
   const float cp0 = P[0] - C[0], cp1 = P[1] - C[1], cp2 = P[2] - C[2];
   const float d5 = ab0 * cp0 + ab1 * cp1 + ab2 * cp2;
   const float d6 = ac0 * cp0 + ac1 * cp1 + ac2 * cp2;
-  if(d6 >= 0.f && d5 <= d6) return cp0 * cp0 + cp1 * cp1 + cp2 * cp2;
+  if(d6 >= 0.f && d5 <= d6) return ret(cp0, cp1, cp2);
   const float vb = d5 * d2 - d1 * d6;
   if(vb <= 0.f && d2 >= 0.f && d6 <= 0.f)
   {
     const float w = d2 / (d2 - d6);
-    const float x = ap0 - w * ac0, y = ap1 - w * ac1, z = ap2 - w * ac2;
-    return x * x + y * y + z * z;
+    return ret(ap0 - w * ac0, ap1 - w * ac1, ap2 - w * ac2);
   }
   const float va = d3 * d6 - d5 * d4;
   if(va <= 0.f && (d4 - d3) >= 0.f && (d5 - d6) >= 0.f)
   {
     const float w = (d4 - d3) / ((d4 - d3) + (d5 - d6));
-    const float x = bp0 - w * (C[0] - B[0]), y = bp1 - w * (C[1] - B[1]), z = bp2 - w * (C[2] - B[2]);
-    return x * x + y * y + z * z;
+    return ret(bp0 - w * (C[0] - B[0]), bp1 - w * (C[1] - B[1]), bp2 - w * (C[2] - B[2]));
   }
   const float denom = 1.f / (va + vb + vc);
   const float v = vb * denom, w = vc * denom;
-  const float x = ap0 - v * ab0 - w * ac0, y = ap1 - v * ab1 - w * ac1, z = ap2 - v * ab2 - w * ac2;
-  return x * x + y * y + z * z;
+  return ret(ap0 - v * ab0 - w * ac0, ap1 - v * ab1 - w * ac1, ap2 - v * ab2 - w * ac2);
 }
 
 // Per-query constants of the FP32 certificates.
@@ -243,7 +245,7 @@ __device__ __forceinline__ int leaf_prefilter(const LeafRec32<NPC>* __restrict__
 // triangles of fine meshes this is ~1e-6, far above rounding); both doubled.
 template <int NPC>
 __device__ __forceinline__ int leaf_prefilter_bounds(const LeafRec32<NPC>* __restrict__ leaves32, int leafpos,
-                                                     const QCtx& c, float& lo2, float& hi2)
+                                                     const QCtx& c, float& lo2, float& hi2, float* cpf, float& rad)
 {
   const float4* r = reinterpret_cast<const float4*>(leaves32 + leafpos);
   float v[3 * NPC];
@@ -264,13 +266,15 @@ __device__ __forceinline__ int leaf_prefilter_bounds(const LeafRec32<NPC>* __res
   int need = 0;
   lo2 = INFINITY;
   hi2 = INFINITY;
+  rad = INFINITY;
 #pragma unroll
   for(int s = 0; s < NPC - 2; ++s)
   {
     const float* A = v;
     const float* B = v + 3 * (s + 1);
     const float* C = v + 3 * (s + 2);
-    const float d2 = dist2_f32(c.qf, A, B, C);
+    float off[3];
+    const float d2 = dist2_f32(c.qf, A, B, C, off);
     const float ap = fmaxf(fabsf(c.qf[0] - A[0]), fmaxf(fabsf(c.qf[1] - A[1]), fabsf(c.qf[2] - A[2])));
     const float E = __fadd_ru(c.lip, __fmul_ru(ec[s], __fadd_ru(ap, lt[s])));
     const float lim = __fadd_ru(c.thr_leaf, E);
@@ -285,6 +289,10 @@ __device__ __forceinline__ int leaf_prefilter_bounds(const LeafRec32<NPC>* __res
       const float l2 = __fmul_rd(dl, dl), h2 = __fmul_ru(dh, dh);
       lo2 = (d2 == d2) ? fminf(lo2, l2) : 0.f;
       hi2 = (d2 == d2 && h2 == h2) ? fminf(hi2, h2) : hi2;
+      // closest point estimate: the exact projection is 1-Lipschitz, so the
+      // FP64 point lies within 2 (E + fz) of qf - off
+      for(int d = 0; d < 3; ++d) cpf[d] = c.qf[d] - off[d];
+      rad = __fmul_ru(2.f, __fadd_ru(E, fz));
     }
   }
   return need;
