@@ -351,6 +351,35 @@ __global__ void __launch_bounds__(128, 5) k_sdf_mixed(const NodeRec64* __restric
           // before it and certainly clears (its point is far from every earlier
           // closest point) leaves the state of checkCandidate independent of
           // all earlier candidates: they are dropped unevaluated.
+          bool noop = false;
+          if(need == 1 || need == 2)
+          {
+            // certainly no update (lo2 >= every possible minimum) and certainly
+            // no pseudo-normal accumulation (far from every possible closest
+            // point): checkCandidate would leave the state unchanged
+            noop = lo2 >= fminf(reset ? INFINITY : mhi, phi) && (reset || np > 0 || mvalid);
+            if(noop && !reset && mvalid) noop = far(cpf, mpf, __fadd_ru(rad, __fmul_ru(0x1p-22f, mesh_max)));
+            for(int j = 0; noop && j < np; ++j) noop = far(cpf, qcp + 3 * j, __fadd_ru(rad, qrad[j]));
+            if(AUDIT && noop)
+            {
+              MinCand s1 = mc;
+              if(reset) init_min(s1);
+              for(int j = 0; j < np; ++j) leaf_refine<NPC>(leaves64, pq[j] >> 2, pq[j] & 3, q, s1, computeNormal);
+              MinCand s2 = s1;
+              leaf_refine<NPC>(leaves64, lp, need, q, s2, computeNormal);
+              const bool same = s1.minSq == s2.minSq && s1.type == s2.type && s1.leaf == s2.leaf &&
+                                s1.sub == s2.sub && s1.mp[0] == s2.mp[0] && s1.mp[1] == s2.mp[1] &&
+                                s1.mp[2] == s2.mp[2] && s1.sn[0] == s2.sn[0] && s1.sn[1] == s2.sn[1] &&
+                                s1.sn[2] == s2.sn[2];
+              if(!same) ++st[0];
+            }
+          }
+          if(noop)
+          {
+            if(AUDIT) ++st[3];
+          }
+          else
+          {
           if(need == 1 || need == 2)
           {
             bool sup = hi2 < fminf(reset ? INFINITY : mlo, plo);
@@ -392,6 +421,7 @@ __global__ void __launch_bounds__(128, 5) k_sdf_mixed(const NodeRec64* __restric
             plo = fminf(plo, lo2);
             phi = fminf(phi, hi2);
             set_thresholds();
+          }
           }
         }
         after_leaf();
