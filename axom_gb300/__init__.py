@@ -23,7 +23,7 @@ from pathlib import Path
 
 import numpy as np
 
-__all__ = ["GsqError", "BVH", "SignedDistance", "load", "PRECISION_FP64", "PRECISION_MIXED"]
+__all__ = ["GsqError", "BVH", "SignedDistance", "Batch", "load", "PRECISION_FP64", "PRECISION_MIXED"]
 
 PKG = Path(__file__).resolve().parent
 LIB_PATH = PKG / "libgsq.so"
@@ -49,6 +49,15 @@ class GsqError(RuntimeError):
 class SdfOpts(C.Structure):
     _fields_ = [("precision", C.c_int32), ("sort_queries", C.c_int32), ("block_size", C.c_int32),
                 ("audit", C.c_int32), ("queue_depth", C.c_int32), ("reserved", C.c_int32 * 3)]
+
+
+class BatchOpts(C.Structure):
+    _fields_ = [("block_size", C.c_int32), ("queue_depth", C.c_int32), ("stack_depth", C.c_int32),
+                ("morton_bits", C.c_int32), ("leaf_size", C.c_int32), ("closest_points", C.c_int32),
+                ("reserved", C.c_int32 * 2)]
+
+    def as_dict(self) -> dict:
+        return {k: getattr(self, k) for k, _ in self._fields_ if k != "reserved"}
 
 
 # (name, restype, argtypes) of every entry point declared in include/gsq.h
@@ -85,6 +94,19 @@ SIGNATURES = [
     ("gsq_sdf_mixed_stats", C.c_int, [_vp, _i64p]),
     ("gsq_sdf_backward", C.c_int, [_vp, _vp, _vp, _vp, C.c_int32, C.c_int32, _vp, _vp, _vp, _vp]),
     ("gsq_sdf_eval_noalloc", C.c_int, [_vp, _vp, _vp, _vp, C.c_int32, C.c_int32, _vp, _vp]),
+    ("gsq_batch_opts_init", C.c_int, [_vp]),
+    ("gsq_batch_create", C.c_int, [C.POINTER(_vp), C.c_int32, _vp, _vp, _vp, C.c_int32, _vp, C.c_int32, C.c_int32,
+                                   _vp, _vp]),
+    ("gsq_batch_destroy", C.c_int, [_vp]),
+    ("gsq_batch_set_vertices", C.c_int, [_vp, _vp, _vp, _vp, _vp]),
+    ("gsq_batch_set_points", C.c_int, [_vp, _vp, _vp]),
+    ("gsq_batch_run", C.c_int, [_vp, _vp, _vp, _vp]),
+    ("gsq_batch_device_output", C.c_int, [_vp, C.POINTER(_vp), C.POINTER(_vp)]),
+    ("gsq_batch_tune", C.c_int, [_vp, _vp]),
+    ("gsq_batch_get_opts", C.c_int, [_vp, _vp]),
+    ("gsq_batch_set_opts", C.c_int, [_vp, _vp]),
+    ("gsq_batch_last_ms", C.c_int, [_vp, C.POINTER(C.c_float)]),
+    ("gsq_batch_max_depth", C.c_int, [_vp, _ip]),
 ]
 NOALLOC_MAX_QUERIES = 262144  # GSQ_NOALLOC_MAX_QUERIES in include/gsq.h
 
@@ -378,4 +400,119 @@ class SignedDistance:
     def last_eval_ms(self) -> float:
         v = C.c_float()
         _check(self._lib.gsq_sdf_last_eval_ms(self._h, C.byref(v)))
+        return v.value
+
+
+class Batch:
+    """Many meshes, each with its own points, evaluated together (the batched
+    form; no reference counterpart).  ``meshes`` is a list of (vertices (V_k, 3),
+    cells (C_k, 3 or 4)) with mesh-local vertex ids; ``points`` a list of
+    (M_k, 3) arrays.  Every run rebuilds all trees and evaluates all points
+    with one CUDA graph launch; each mesh's results equal ``SignedDistance``
+    on that mesh alone (MIXED or FP64: they agree bit for bit)."""
+
+    def __init__(self, meshes, points, is_watertight: bool = True, compute_sign: bool = True,
+                 closest_points: bool = False, **opts):
+        self._lib = load()
+        verts = [np.ascontiguousarray(v, dtype=np.float64).reshape(-1, 3) for v, _ in meshes]
+        cells = [np.ascontiguousarray(c, dtype=np.int32) for _, c in meshes]
+        npc = cells[0].shape[1]
+        if any(c.shape[1] != npc for c in cells):
+            raise ValueError("all meshes need the same nodes per cell")
+        sizes = [int(np.asarray(p).reshape(-1, 3).shape[0]) if not _is_torch(p) else int(p.reshape(-1, 3).shape[0])
+                 for p in points]
+        self.vert_offsets = np.concatenate([[0], np.cumsum([v.shape[0] for v in verts])]).astype(np.int64)
+        self.cell_offsets = np.concatenate([[0], np.cumsum([c.shape[0] for c in cells])]).astype(np.int64)
+        self.point_offsets = np.concatenate([[0], np.cumsum(sizes)]).astype(np.int64)
+        self.num_points = int(self.point_offsets[-1])
+        allc = np.ascontiguousarray(np.concatenate(cells), dtype=np.int32)
+        o = BatchOpts()
+        _check(self._lib.gsq_batch_opts_init(C.byref(o)))
+        for k, v in opts.items():
+            setattr(o, k, int(v))
+        o.closest_points = int(closest_points)
+        h = _vp()
+        _check(self._lib.gsq_batch_create(C.byref(h), len(meshes), C.c_void_p(self.vert_offsets.ctypes.data),
+                                          C.c_void_p(self.cell_offsets.ctypes.data), C.c_void_p(allc.ctypes.data),
+                                          npc, C.c_void_p(self.point_offsets.ctypes.data), int(is_watertight),
+                                          int(compute_sign), C.byref(o), _stream()))
+        self._h = h
+        self.closest_points = closest_points
+        self.set_vertices(np.concatenate(verts))
+        self.set_points(points)
+
+    def __del__(self):
+        if getattr(self, "_h", None):
+            self._lib.gsq_batch_destroy(self._h)
+            self._h = None
+
+    def set_vertices(self, vertices):
+        """All meshes' vertices: a (sum V_k, 3) host array, or a tuple (x, y, z)
+        of contiguous float64 arrays or tensors (host, pinned or device)."""
+        if isinstance(vertices, tuple):
+            xyz = [_Arr(a, np.float64) for a in vertices]
+        else:
+            v = np.ascontiguousarray(np.asarray(vertices, dtype=np.float64).reshape(-1, 3).T)
+            xyz = [_Arr(v[k], np.float64) for k in range(3)]
+        _check(self._lib.gsq_batch_set_vertices(self._h, *[C.c_void_p(a.ptr) for a in xyz], _stream()))
+
+    def set_points(self, points):
+        """A list of per-mesh (M_k, 3) arrays, or one (sum M_k, 3) array (host or device)."""
+        if isinstance(points, (list, tuple)):
+            if points and _is_torch(points[0]):
+                import torch
+                points = torch.cat([p.reshape(-1, 3) for p in points])
+            else:
+                points = np.concatenate([np.asarray(p, dtype=np.float64).reshape(-1, 3) for p in points])
+        p = _Arr(points, np.float64, 3)
+        if p.n != self.num_points:
+            raise ValueError(f"expected {self.num_points} points, got {p.n}")
+        self._points = p  # keeps a converted copy alive until the copy is done
+        _check(self._lib.gsq_batch_set_points(self._h, C.c_void_p(p.ptr), _stream()))
+
+    def run(self, out=None, closest=None):
+        """Rebuilds every tree and evaluates every point.  Returns the distances
+        (into ``out`` if given, else a new host array) and, if ``closest`` is
+        True or an array, the closest points."""
+        out = np.empty(self.num_points) if out is None else out
+        if closest is True:
+            closest = np.empty((self.num_points, 3))
+        _check(self._lib.gsq_batch_run(self._h, C.c_void_p(_ptr(out)) if out is not False else None,
+                                       C.c_void_p(_ptr(closest)) if closest is not None and closest is not False
+                                       else None, _stream()))
+        return (out, closest) if closest is not None and closest is not False else out
+
+    def run_device(self):
+        """Runs and leaves the results on the device; returns the last run's milliseconds."""
+        _check(self._lib.gsq_batch_run(self._h, None, None, _stream()))
+        return self.last_ms()
+
+    def split(self, flat):
+        """Per-mesh views of a flat per-point array."""
+        return [flat[a:b] for a, b in zip(self.point_offsets[:-1], self.point_offsets[1:])]
+
+    def tune(self) -> dict:
+        _check(self._lib.gsq_batch_tune(self._h, _stream()))
+        return self.opts()
+
+    def opts(self) -> dict:
+        o = BatchOpts()
+        _check(self._lib.gsq_batch_get_opts(self._h, C.byref(o)))
+        return o.as_dict()
+
+    def set_opts(self, **kw):
+        o = BatchOpts()
+        _check(self._lib.gsq_batch_get_opts(self._h, C.byref(o)))
+        for k, v in kw.items():
+            setattr(o, k, int(v))
+        _check(self._lib.gsq_batch_set_opts(self._h, C.byref(o)))
+
+    def last_ms(self) -> float:
+        v = C.c_float()
+        _check(self._lib.gsq_batch_last_ms(self._h, C.byref(v)))
+        return v.value
+
+    def max_depth(self) -> int:
+        v = C.c_int32()
+        _check(self._lib.gsq_batch_max_depth(self._h, C.byref(v)))
         return v.value

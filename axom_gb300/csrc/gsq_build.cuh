@@ -1,0 +1,334 @@
+// Device pieces of the linear BVH build, shared by the single-hierarchy build
+// (gsq_bvh.cu) and the segmented build of many meshes (gsq_batch.cu).  Every
+// function works on one hierarchy given by base pointers and local indices,
+// so a segmented build produces, per mesh, the same bits as a standalone one.
+#pragma once
+
+#include "gsq_internal.cuh"
+
+#include <climits>
+
+namespace gsq
+{
+namespace lbvh
+{
+// (value, index) pairs folded "leftmost wins on ties", which reproduces the
+// strict-comparison updates of BoundingBox::addPoint applied in index order.
+struct ArgV
+{
+  double v;
+  int i;
+};
+__device__ __forceinline__ void take_min(ArgV& a, const ArgV& b)
+{
+  if(b.i != INT_MAX && (a.i == INT_MAX || b.v < a.v || (b.v == a.v && b.i < a.i))) a = b;
+}
+__device__ __forceinline__ void take_max(ArgV& a, const ArgV& b)
+{
+  if(b.i != INT_MAX && (a.i == INT_MAX || b.v > a.v || (b.v == a.v && b.i < a.i))) a = b;
+}
+__device__ __forceinline__ ArgV shfl_argv(const ArgV& a, int src)
+{
+  return ArgV {__shfl_sync(0xFFFFFFFFu, a.v, src), __shfl_sync(0xFFFFFFFFu, a.i, src)};
+}
+
+struct Fold
+{
+  ArgV lo[3], hi[3];
+  int first_valid;
+};
+
+__device__ __forceinline__ void fold_init(Fold& f)
+{
+  for(int d = 0; d < 3; ++d)
+  {
+    f.lo[d] = ArgV {0.0, INT_MAX};
+    f.hi[d] = ArgV {0.0, INT_MAX};
+  }
+  f.first_valid = INT_MAX;
+}
+
+__device__ __forceinline__ void fold_merge(Fold& a, const Fold& b)
+{
+  for(int d = 0; d < 3; ++d)
+  {
+    take_min(a.lo[d], b.lo[d]);
+    take_max(a.hi[d], b.hi[d]);
+  }
+  a.first_valid = min(a.first_valid, b.first_valid);
+}
+
+__device__ __forceinline__ void fold_warp(Fold& f)
+{
+  const int lane = threadIdx.x & 31;
+  for(int off = 16; off > 0; off >>= 1)
+  {
+    const int src = lane + off < 32 ? lane + off : lane;
+    Fold o;
+    for(int d = 0; d < 3; ++d)
+    {
+      o.lo[d] = shfl_argv(f.lo[d], src);
+      o.hi[d] = shfl_argv(f.hi[d], src);
+    }
+    o.first_valid = __shfl_sync(0xFFFFFFFFu, f.first_valid, src);
+    fold_merge(f, o);
+  }
+}
+
+// Folds a whole block (blockDim.x a multiple of 32, at most 1024); the result
+// is valid in thread 0.
+__device__ __forceinline__ Fold fold_block(Fold f)
+{
+  __shared__ Fold s_f[32];
+  fold_warp(f);
+  if((threadIdx.x & 31) == 0) s_f[threadIdx.x >> 5] = f;
+  __syncthreads();
+  Fold a = s_f[0];
+  if(threadIdx.x == 0)
+    for(int w = 1; w < (int)(blockDim.x >> 5); ++w) fold_merge(a, s_f[w]);
+  __syncthreads();
+  return a;
+}
+
+// BoundingBox::scale (BoundingBox.hpp:548-561): mid = 0.5*(lo+hi),
+// r = (s*0.5)*(hi-lo), lo' = mid - r, hi' = mid + r, then checkAndFixBounds.
+// Invalid boxes are left as they are.  Returns the box's validity.
+__device__ __forceinline__ bool scale_box(double* lo, double* hi, double half)
+{
+  const bool valid = box_valid(lo, hi);
+  if(valid)
+  {
+    for(int d = 0; d < 3; ++d)
+    {
+      const double mid = 0.5 * (lo[d] + hi[d]);
+      const double r = (hi[d] - lo[d]) * half;
+      lo[d] = mid - r;
+      hi[d] = mid + r;
+    }
+    for(int d = 0; d < 3; ++d)
+      if(lo[d] > hi[d])
+      {
+        const double t = lo[d];
+        lo[d] = hi[d];
+        hi[d] = t;
+      }
+  }
+  return valid;
+}
+
+// One valid scaled box into the bounds fold (reduce, SEQ branch, BR:134-141:
+// addBox from an invalid box = per-axis leftmost min of lo and leftmost max of
+// "lo if lo == hi else hi", the first valid box contributing its own hi).
+__device__ __forceinline__ void fold_add_box(Fold& f, const double* lo, const double* hi, int i)
+{
+  for(int d = 0; d < 3; ++d)
+  {
+    take_min(f.lo[d], ArgV {lo[d], i});
+    take_max(f.hi[d], ArgV {(lo[d] == hi[d]) ? lo[d] : hi[d], i});
+  }
+  f.first_valid = min(f.first_valid, i);
+}
+
+// Bounds and Morton parameters from the folded boxes.  leaf holds the scaled
+// boxes addressed by the fold's indices; last is the index of the last box
+// (the fold's result when no box is valid).  params: bounds lo[3] hi[3], then
+// Morton min[3], inv_extent[3].
+__device__ __forceinline__ void bounds_params(const Fold& a, const double* __restrict__ leaf, int last,
+                                              double* __restrict__ params)
+{
+  double lo[3], hi[3];
+  if(a.first_valid == INT_MAX)
+  {
+    for(int d = 0; d < 3; ++d)
+    {
+      lo[d] = leaf[6 * (size_t)last + d];
+      hi[d] = leaf[6 * (size_t)last + 3 + d];
+    }
+  }
+  else
+  {
+    for(int d = 0; d < 3; ++d)
+    {
+      lo[d] = a.lo[d].v;
+      hi[d] = (a.hi[d].i == a.first_valid) ? leaf[6 * (size_t)a.first_valid + 3 + d] : a.hi[d].v;
+    }
+  }
+  for(int d = 0; d < 3; ++d)
+  {
+    params[d] = lo[d];
+    params[3 + d] = hi[d];
+    // get_mcodes (BR:154-163): inv_extent = isNearlyEqual(extent, 0) ? 0 : 1/extent
+    const double ext = hi[d] - lo[d];
+    params[6 + d] = lo[d];
+    params[9 + d] = (fabs(ext - 0.0) <= 1.0e-8) ? 0.0 : 1.0 / ext;
+  }
+}
+
+// 10-bit spread for a 3D Morton interleave (Ericson's magic numbers; the
+// reference's Mortonizer<int32,int32,3>::expandBits, spin/MortonIndex.hpp:151-159).
+__host__ __device__ __forceinline__ uint32_t spread10(uint32_t x)
+{
+  x = (x | (x << 16)) & 0xFF0000FFu;
+  x = (x | (x << 8)) & 0x0F00F00Fu;
+  x = (x | (x << 4)) & 0xC30C30C3u;
+  x = (x | (x << 2)) & 0x49249249u;
+  return x;
+}
+
+// morton32_encode (BR:48-65) of the normalised centroid (BR:165-175).
+__device__ __forceinline__ uint32_t box_morton(const double* __restrict__ box, const double* __restrict__ params)
+{
+  uint32_t q[3];
+  for(int d = 0; d < 3; ++d)
+  {
+    const double mid = 0.5 * (box[d] + box[3 + d]);
+    const double c = (mid - params[6 + d]) * params[9 + d];
+    q[d] = (uint32_t)(int)fmin(fmax(c * 1024.0, 0.0), 1023.0);
+  }
+  return spread10(q[0]) | (spread10(q[1]) << 1) | (spread10(q[2]) << 2);
+}
+
+// delta (BR:265-287)
+__device__ __forceinline__ int delta(int a, int b, int inner, const uint32_t* __restrict__ codes)
+{
+  const bool oor = (b < 0 || b > inner);
+  const int bb = oor ? 0 : b;
+  uint32_t x = __ldg(codes + a) ^ __ldg(codes + bb);
+  const bool tie = (x == 0);
+  if(tie) x = (uint32_t)a ^ (uint32_t)bb;
+  int c = __clz(x);
+  if(tie) c += 32;
+  return oor ? -1 : c;
+}
+
+// build_tree (BR:290-384) for inner node i of a hierarchy over n sorted codes;
+// also writes the child links of the node record.  Leaf j has node id
+// inner + j in lchild/rchild/parent.
+__device__ __forceinline__ void karras_node(int i, const uint32_t* __restrict__ codes, int n, int* __restrict__ lchild,
+                                            int* __restrict__ rchild, int* __restrict__ parent,
+                                            NodeRec64* __restrict__ nodes)
+{
+  const int inner = n - 1;
+  const int dir = (delta(i, i + 1, inner, codes) - delta(i, i - 1, inner, codes)) < 0 ? -1 : 1;
+  const int dmin = delta(i, i - dir, inner, codes);
+  int lmax = 2;
+  while(delta(i, i + lmax * dir, inner, codes) > dmin) lmax *= 2;
+  int l = 0;
+  for(int s = lmax / 2; s >= 1; s /= 2)
+    if(delta(i, i + (l + s) * dir, inner, codes) > dmin) l += s;
+  const int j = i + l * dir;
+  const int dnode = delta(i, j, inner, codes);
+  int s = 0;
+  double div = 2.0;
+  for(int st = (int)ceil(double(float(l)) / div);; div *= 2.0, st = (int)ceil(double(float(l)) / div))
+  {
+    if(delta(i, i + (s + st) * dir, inner, codes) > dnode) s += st;
+    if(st == 1) break;
+  }
+  const int split = i + s * dir + min(dir, 0);
+  int lc, rc;
+  if(min(i, j) == split)
+  {
+    parent[split + inner] = i;
+    lc = split + inner;
+  }
+  else
+  {
+    parent[split] = i;
+    lc = split;
+  }
+  if(max(i, j) == split + 1)
+  {
+    parent[split + inner + 1] = i;
+    rc = split + inner + 1;
+  }
+  else
+  {
+    parent[split + 1] = i;
+    rc = split + 1;
+  }
+  lchild[i] = lc;
+  rchild[i] = rc;
+  nodes[i].child[0] = (lc >= inner) ? -(lc - inner + 1) : lc;
+  nodes[i].child[1] = (rc >= inner) ? -(rc - inner + 1) : rc;
+  if(i == 0) parent[0] = -1;
+}
+
+// BoundingBox::addBox (BoundingBox.hpp:487-505) into acc.
+__device__ __forceinline__ void add_box(double* alo, double* ahi, const double* lo, const double* hi)
+{
+  if(box_valid(alo, ahi))
+  {
+    if(box_valid(lo, hi))
+    {
+      for(int d = 0; d < 3; ++d)
+      {
+        if(lo[d] < alo[d]) alo[d] = lo[d];
+        if(lo[d] > ahi[d]) ahi[d] = lo[d];
+      }
+      for(int d = 0; d < 3; ++d)
+      {
+        if(hi[d] < alo[d]) alo[d] = hi[d];
+        if(hi[d] > ahi[d]) ahi[d] = hi[d];
+      }
+    }
+  }
+  else
+    for(int d = 0; d < 3; ++d)
+    {
+      alo[d] = lo[d];
+      ahi[d] = hi[d];
+    }
+}
+
+// propagate_aabbs (BR:505-576) fused with emit_bvh_parents (LB:225-264), for
+// sorted leaf k with box (lo, hi) of a hierarchy over n leaves.  The thread
+// stores its box into its parent's record, fences, and bumps the parent's
+// counter; the first arrival exits and the second combines the two child
+// boxes as the reference's SEQ order does (box(node) = addBox(box(right),
+// box(left))) and moves up.  No thread ever waits on another.
+__device__ __forceinline__ void refit_leaf(int k, double* lo, double* hi, int n, const int* __restrict__ lchild,
+                                           const int* __restrict__ parent, int* __restrict__ counters,
+                                           NodeRec64* nodes, double* __restrict__ root_box)
+{
+  const int inner = n - 1;
+  int last = inner + k;
+  int node = parent[inner + k];
+  while(true)
+  {
+    const int side = (lchild[node] == last) ? 0 : 1;
+    double* dst = nodes[node].b + 6 * side;
+    for(int d = 0; d < 3; ++d)
+    {
+      dst[d] = lo[d];
+      dst[3 + d] = hi[d];
+    }
+    __threadfence();
+    if(atomicAdd(&counters[node], 1) == 0) return;
+    __threadfence();
+    const double* b = nodes[node].b;
+    double llo[3], lhi[3];
+    for(int d = 0; d < 3; ++d)
+    {
+      lo[d] = __ldcg(b + 6 + d);  // right child box
+      hi[d] = __ldcg(b + 9 + d);
+      llo[d] = __ldcg(b + d);     // left child box
+      lhi[d] = __ldcg(b + 3 + d);
+    }
+    add_box(lo, hi, llo, lhi);
+    last = node;
+    node = parent[node];
+    if(node == -1)
+    {
+      if(root_box)
+        for(int d = 0; d < 3; ++d)
+        {
+          root_box[d] = lo[d];
+          root_box[3 + d] = hi[d];
+        }
+      return;
+    }
+  }
+}
+}  // namespace lbvh
+}  // namespace gsq

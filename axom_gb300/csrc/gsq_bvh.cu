@@ -20,7 +20,7 @@
 // pass 1 keeps up to CAP candidates per query in scratch and counts all of
 // them, a scan gives the CSR offsets, and pass 2 copies, re-traversing only
 // the queries with more than CAP candidates.
-#include "gsq_internal.cuh"
+#include "gsq_build.cuh"
 
 #include <algorithm>
 #include <climits>
@@ -36,74 +36,16 @@ namespace
 {
 constexpr int BUILD_THREADS = 256;
 
-// (value, index) pairs folded "leftmost wins on ties", which reproduces the
-// strict-comparison updates of BoundingBox::addPoint applied in index order.
-struct ArgV
-{
-  double v;
-  int i;
-};
-__device__ __forceinline__ void take_min(ArgV& a, const ArgV& b)
-{
-  if(b.i != INT_MAX && (a.i == INT_MAX || b.v < a.v || (b.v == a.v && b.i < a.i))) a = b;
-}
-__device__ __forceinline__ void take_max(ArgV& a, const ArgV& b)
-{
-  if(b.i != INT_MAX && (a.i == INT_MAX || b.v > a.v || (b.v == a.v && b.i < a.i))) a = b;
-}
-__device__ __forceinline__ ArgV shfl_argv(const ArgV& a, int src)
-{
-  return ArgV {__shfl_sync(0xFFFFFFFFu, a.v, src), __shfl_sync(0xFFFFFFFFu, a.i, src)};
-}
+using lbvh::ArgV;
+using lbvh::Fold;
+using lbvh::fold_block;
+using lbvh::fold_init;
+using lbvh::fold_merge;
+using lbvh::take_max;
+using lbvh::take_min;
 
-struct Fold
-{
-  ArgV lo[3], hi[3];
-  int first_valid;
-};
-
-__device__ __forceinline__ void fold_init(Fold& f)
-{
-  for(int d = 0; d < 3; ++d)
-  {
-    f.lo[d] = ArgV {0.0, INT_MAX};
-    f.hi[d] = ArgV {0.0, INT_MAX};
-  }
-  f.first_valid = INT_MAX;
-}
-
-__device__ __forceinline__ void fold_merge(Fold& a, const Fold& b)
-{
-  for(int d = 0; d < 3; ++d)
-  {
-    take_min(a.lo[d], b.lo[d]);
-    take_max(a.hi[d], b.hi[d]);
-  }
-  a.first_valid = min(a.first_valid, b.first_valid);
-}
-
-__device__ __forceinline__ void fold_warp(Fold& f)
-{
-  for(int off = 16; off > 0; off >>= 1)
-  {
-    Fold o;
-    for(int d = 0; d < 3; ++d)
-    {
-      o.lo[d] = shfl_argv(f.lo[d], (threadIdx.x & 31) + off < 32 ? (threadIdx.x & 31) + off : (threadIdx.x & 31));
-      o.hi[d] = shfl_argv(f.hi[d], (threadIdx.x & 31) + off < 32 ? (threadIdx.x & 31) + off : (threadIdx.x & 31));
-    }
-    o.first_valid = __shfl_sync(0xFFFFFFFFu, f.first_valid,
-                                (threadIdx.x & 31) + off < 32 ? (threadIdx.x & 31) + off : (threadIdx.x & 31));
-    fold_merge(f, o);
-  }
-}
-
-// Scaled leaf boxes + per-block folds of the bounds.
-//   BoundingBox::scale (BoundingBox.hpp:548-561): mid = 0.5*(lo+hi),
-//   r = (s*0.5)*(hi-lo), lo' = mid - r, hi' = mid + r, then checkAndFixBounds.
-//   reduce, SEQ branch (BR:134-141): addBox fold from an invalid box, i.e. the
-//   per-axis leftmost min of lo and leftmost max of "lo if lo == hi else hi"
-//   over valid boxes, with the first valid box contributing its own hi.
+// Scaled leaf boxes + per-block folds of the bounds (transform_boxes, BR:85-99,
+// and reduce, BR:102-143).
 __global__ void __launch_bounds__(BUILD_THREADS) k_leaf_bounds(const double* __restrict__ in,
                                                                  int n,
                                                                  double scale,
@@ -121,96 +63,31 @@ __global__ void __launch_bounds__(BUILD_THREADS) k_leaf_bounds(const double* __r
       lo[d] = in[6 * (size_t)i + d];
       hi[d] = in[6 * (size_t)i + 3 + d];
     }
-    const bool valid = box_valid(lo, hi);
-    if(valid)
-    {
-      for(int d = 0; d < 3; ++d)
-      {
-        const double mid = 0.5 * (lo[d] + hi[d]);
-        const double r = (hi[d] - lo[d]) * half;
-        lo[d] = mid - r;
-        hi[d] = mid + r;
-      }
-      for(int d = 0; d < 3; ++d)
-        if(lo[d] > hi[d])
-        {
-          const double t = lo[d];
-          lo[d] = hi[d];
-          hi[d] = t;
-        }
-      for(int d = 0; d < 3; ++d)
-      {
-        take_min(f.lo[d], ArgV {lo[d], i});
-        take_max(f.hi[d], ArgV {(lo[d] == hi[d]) ? lo[d] : hi[d], i});
-      }
-      f.first_valid = min(f.first_valid, i);
-    }
+    if(lbvh::scale_box(lo, hi, half)) lbvh::fold_add_box(f, lo, hi, i);
     for(int d = 0; d < 3; ++d)
     {
       leaf[6 * (size_t)i + d] = lo[d];
       leaf[6 * (size_t)i + 3 + d] = hi[d];
     }
   }
-  fold_warp(f);
-  __shared__ Fold s_f[BUILD_THREADS / 32];
-  if((threadIdx.x & 31) == 0) s_f[threadIdx.x >> 5] = f;
-  __syncthreads();
-  if(threadIdx.x == 0)
-  {
-    Fold a = s_f[0];
-    for(int w = 1; w < BUILD_THREADS / 32; ++w) fold_merge(a, s_f[w]);
-    partials[blockIdx.x] = a;
-  }
+  const Fold a = fold_block(f);
+  if(threadIdx.x == 0) partials[blockIdx.x] = a;
 }
 
 // params: bounds lo[3] hi[3], then Morton min[3], inv_extent[3].
-__global__ void k_bounds_final(const Fold* __restrict__ partials, int nb, const double* __restrict__ leaf, int n,
-                               double* __restrict__ params)
+// One block: the partial folds merged across the block (the merge is
+// commutative: it keeps the leftmost extreme).
+__global__ void __launch_bounds__(BUILD_THREADS) k_bounds_final(const Fold* __restrict__ partials, int nb,
+                                                                  const double* __restrict__ leaf, int n,
+                                                                  double* __restrict__ params)
 {
-  if(threadIdx.x != 0 || blockIdx.x != 0) return;
-  Fold a = partials[0];
-  for(int b = 1; b < nb; ++b) fold_merge(a, partials[b]);
-  double lo[3], hi[3];
-  if(a.first_valid == INT_MAX)
-  {
-    // no valid box: the fold ends as a copy of the last box
-    for(int d = 0; d < 3; ++d)
-    {
-      lo[d] = leaf[6 * (size_t)(n - 1) + d];
-      hi[d] = leaf[6 * (size_t)(n - 1) + 3 + d];
-    }
-  }
-  else
-  {
-    for(int d = 0; d < 3; ++d)
-    {
-      lo[d] = a.lo[d].v;
-      hi[d] = (a.hi[d].i == a.first_valid) ? leaf[6 * (size_t)a.first_valid + 3 + d] : a.hi[d].v;
-    }
-  }
-  for(int d = 0; d < 3; ++d)
-  {
-    params[d] = lo[d];
-    params[3 + d] = hi[d];
-    // get_mcodes (BR:154-163): inv_extent = isNearlyEqual(extent, 0) ? 0 : 1/extent
-    const double ext = hi[d] - lo[d];
-    params[6 + d] = lo[d];
-    params[9 + d] = (fabs(ext - 0.0) <= 1.0e-8) ? 0.0 : 1.0 / ext;
-  }
+  Fold f;
+  fold_init(f);
+  for(int b = threadIdx.x; b < nb; b += blockDim.x) fold_merge(f, partials[b]);
+  const Fold a = fold_block(f);
+  if(threadIdx.x == 0) lbvh::bounds_params(a, leaf, n - 1, params);
 }
 
-// 10-bit spread for a 3D Morton interleave (Ericson's magic numbers; the
-// reference's Mortonizer<int32,int32,3>::expandBits, spin/MortonIndex.hpp:151-159).
-__device__ __forceinline__ uint32_t spread10(uint32_t x)
-{
-  x = (x | (x << 16)) & 0xFF0000FFu;
-  x = (x | (x << 8)) & 0x0F00F00Fu;
-  x = (x | (x << 4)) & 0xC30C30C3u;
-  x = (x | (x << 2)) & 0x49249249u;
-  return x;
-}
-
-// morton32_encode (BR:48-65) of the normalised centroid (BR:165-175).
 __global__ void __launch_bounds__(BUILD_THREADS) k_morton(const double* __restrict__ leaf,
                                                             int n,
                                                             const double* __restrict__ params,
@@ -218,30 +95,9 @@ __global__ void __launch_bounds__(BUILD_THREADS) k_morton(const double* __restri
 {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if(i >= n) return;
-  uint32_t q[3];
-  for(int d = 0; d < 3; ++d)
-  {
-    const double mid = 0.5 * (leaf[6 * (size_t)i + d] + leaf[6 * (size_t)i + 3 + d]);
-    const double c = (mid - params[6 + d]) * params[9 + d];
-    q[d] = (uint32_t)(int)fmin(fmax(c * 1024.0, 0.0), 1023.0);
-  }
-  codes[i] = spread10(q[0]) | (spread10(q[1]) << 1) | (spread10(q[2]) << 2);
+  codes[i] = lbvh::box_morton(leaf + 6 * (size_t)i, params);
 }
 
-// delta (BR:265-287)
-__device__ __forceinline__ int delta(int a, int b, int inner, const uint32_t* __restrict__ codes)
-{
-  const bool oor = (b < 0 || b > inner);
-  const int bb = oor ? 0 : b;
-  uint32_t x = __ldg(codes + a) ^ __ldg(codes + bb);
-  const bool tie = (x == 0);
-  if(tie) x = (uint32_t)a ^ (uint32_t)bb;
-  int c = __clz(x);
-  if(tie) c += 32;
-  return oor ? -1 : c;
-}
-
-// build_tree (BR:290-384); also writes the child links of each node record.
 __global__ void __launch_bounds__(BUILD_THREADS) k_karras(const uint32_t* __restrict__ codes,
                                                             int n,
                                                             int* __restrict__ lchild,
@@ -249,86 +105,12 @@ __global__ void __launch_bounds__(BUILD_THREADS) k_karras(const uint32_t* __rest
                                                             int* __restrict__ parent,
                                                             NodeRec64* __restrict__ nodes)
 {
-  const int inner = n - 1;
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if(i >= inner) return;
-  const int dir = (delta(i, i + 1, inner, codes) - delta(i, i - 1, inner, codes)) < 0 ? -1 : 1;
-  const int dmin = delta(i, i - dir, inner, codes);
-  int lmax = 2;
-  while(delta(i, i + lmax * dir, inner, codes) > dmin) lmax *= 2;
-  int l = 0;
-  for(int s = lmax / 2; s >= 1; s /= 2)
-    if(delta(i, i + (l + s) * dir, inner, codes) > dmin) l += s;
-  const int j = i + l * dir;
-  const int dnode = delta(i, j, inner, codes);
-  int s = 0;
-  double div = 2.0;
-  for(int st = (int)ceil(double(float(l)) / div);; div *= 2.0, st = (int)ceil(double(float(l)) / div))
-  {
-    if(delta(i, i + (s + st) * dir, inner, codes) > dnode) s += st;
-    if(st == 1) break;
-  }
-  const int split = i + s * dir + min(dir, 0);
-  int lc, rc;
-  if(min(i, j) == split)
-  {
-    parent[split + inner] = i;
-    lc = split + inner;
-  }
-  else
-  {
-    parent[split] = i;
-    lc = split;
-  }
-  if(max(i, j) == split + 1)
-  {
-    parent[split + inner + 1] = i;
-    rc = split + inner + 1;
-  }
-  else
-  {
-    parent[split + 1] = i;
-    rc = split + 1;
-  }
-  lchild[i] = lc;
-  rchild[i] = rc;
-  nodes[i].child[0] = (lc >= inner) ? -(lc - inner + 1) : lc;
-  nodes[i].child[1] = (rc >= inner) ? -(rc - inner + 1) : rc;
-  if(i == 0) parent[0] = -1;
+  if(i >= n - 1) return;
+  lbvh::karras_node(i, codes, n, lchild, rchild, parent, nodes);
 }
 
-// BoundingBox::addBox (BoundingBox.hpp:487-505) into acc.
-__device__ __forceinline__ void add_box(double* alo, double* ahi, const double* lo, const double* hi)
-{
-  if(box_valid(alo, ahi))
-  {
-    if(box_valid(lo, hi))
-    {
-      for(int d = 0; d < 3; ++d)
-      {
-        if(lo[d] < alo[d]) alo[d] = lo[d];
-        if(lo[d] > ahi[d]) ahi[d] = lo[d];
-      }
-      for(int d = 0; d < 3; ++d)
-      {
-        if(hi[d] < alo[d]) alo[d] = hi[d];
-        if(hi[d] > ahi[d]) ahi[d] = hi[d];
-      }
-    }
-  }
-  else
-    for(int d = 0; d < 3; ++d)
-    {
-      alo[d] = lo[d];
-      ahi[d] = hi[d];
-    }
-}
-
-// propagate_aabbs (BR:505-576) fused with emit_bvh_parents (LB:225-264).
-// One thread per sorted leaf.  A thread stores its box into its parent's
-// record, fences, and bumps the parent's counter; the first arrival exits and
-// the second combines the two child boxes as the reference's SEQ order does
-// (box(node) = addBox(box(right), box(left))) and moves up.
+// One thread per sorted leaf (lbvh::refit_leaf).
 __global__ void __launch_bounds__(BUILD_THREADS) k_refit(const double* __restrict__ leaf,
                                                            const int* __restrict__ perm,
                                                            int n,
@@ -338,7 +120,6 @@ __global__ void __launch_bounds__(BUILD_THREADS) k_refit(const double* __restric
                                                            NodeRec64* nodes,
                                                            double* __restrict__ root_box)
 {
-  const int inner = n - 1;
   const int k = blockIdx.x * blockDim.x + threadIdx.x;
   if(k >= n) return;
   const int id = perm[k];
@@ -348,42 +129,7 @@ __global__ void __launch_bounds__(BUILD_THREADS) k_refit(const double* __restric
     lo[d] = leaf[6 * (size_t)id + d];
     hi[d] = leaf[6 * (size_t)id + 3 + d];
   }
-  int last = inner + k;
-  int node = parent[inner + k];
-  while(true)
-  {
-    const int side = (lchild[node] == last) ? 0 : 1;
-    double* dst = nodes[node].b + 6 * side;
-    for(int d = 0; d < 3; ++d)
-    {
-      dst[d] = lo[d];
-      dst[3 + d] = hi[d];
-    }
-    __threadfence();
-    if(atomicAdd(&counters[node], 1) == 0) return;
-    __threadfence();
-    const double* b = nodes[node].b;
-    double llo[3], lhi[3];
-    for(int d = 0; d < 3; ++d)
-    {
-      lo[d] = __ldcg(b + 6 + d);   // right child box
-      hi[d] = __ldcg(b + 9 + d);
-      llo[d] = __ldcg(b + d);      // left child box
-      lhi[d] = __ldcg(b + 3 + d);
-    }
-    add_box(lo, hi, llo, lhi);
-    last = node;
-    node = parent[node];
-    if(node == -1)
-    {
-      for(int d = 0; d < 3; ++d)
-      {
-        root_box[d] = lo[d];
-        root_box[3 + d] = hi[d];
-      }
-      return;
-    }
-  }
+  lbvh::refit_leaf(k, lo, hi, n, lchild, parent, counters, nodes, root_box);
 }
 
 // ---- traversal --------------------------------------------------------------
@@ -618,23 +364,18 @@ __global__ void __launch_bounds__(BUILD_THREADS) k_node_fold(const double* __res
       take_max(f.hi[d], ArgV {p[d], i});
     }
   }
-  fold_warp(f);
-  __shared__ Fold s_f[BUILD_THREADS / 32];
-  if((threadIdx.x & 31) == 0) s_f[threadIdx.x >> 5] = f;
-  __syncthreads();
-  if(threadIdx.x == 0)
-  {
-    Fold a = s_f[0];
-    for(int w = 1; w < BUILD_THREADS / 32; ++w) fold_merge(a, s_f[w]);
-    partials[blockIdx.x] = a;
-  }
+  const Fold a = fold_block(f);
+  if(threadIdx.x == 0) partials[blockIdx.x] = a;
 }
 
-__global__ void k_node_final(const Fold* __restrict__ partials, int nb, double* __restrict__ out)
+__global__ void __launch_bounds__(BUILD_THREADS) k_node_final(const Fold* __restrict__ partials, int nb,
+                                                                double* __restrict__ out)
 {
-  if(threadIdx.x != 0 || blockIdx.x != 0) return;
-  Fold a = partials[0];
-  for(int b = 1; b < nb; ++b) fold_merge(a, partials[b]);
+  Fold f;
+  fold_init(f);
+  for(int b = threadIdx.x; b < nb; b += blockDim.x) fold_merge(f, partials[b]);
+  const Fold a = fold_block(f);
+  if(threadIdx.x != 0) return;
   for(int d = 0; d < 3; ++d)
   {
     out[d] = (a.lo[d].i == INT_MAX) ? DBL_MAX : a.lo[d].v;
@@ -652,7 +393,7 @@ int node_bounds(const double* x, const double* y, const double* z, int nv, doubl
   Fold* folds = work.as<Fold>();
   double* d_out = reinterpret_cast<double*>(reinterpret_cast<char*>(folds) + ((sizeof(Fold) * nb + 15) & ~size_t(15)));
   k_node_fold<<<nb, BUILD_THREADS, 0, s>>>(x, y, z, nv, folds);
-  k_node_final<<<1, 32, 0, s>>>(folds, nb, d_out);
+  k_node_final<<<1, BUILD_THREADS, 0, s>>>(folds, nb, d_out);
   count_launch(2);
   GSQ_CUDA_TRY(cudaGetLastError());
   GSQ_CUDA_TRY(cudaMemcpyAsync(out6, d_out, sizeof(double) * 6, cudaMemcpyDeviceToHost, s));
@@ -740,7 +481,7 @@ int bvh_build(BvhDev& B, const double* d_boxes, int n, double scale, cudaStream_
   Fold* folds = reinterpret_cast<Fold*>(w);
 
   k_leaf_bounds<<<fold_blocks, BUILD_THREADS, 0, s>>>(d_boxes, n, scale, leaf, folds);
-  k_bounds_final<<<1, 32, 0, s>>>(folds, fold_blocks, leaf, n, params);
+  k_bounds_final<<<1, BUILD_THREADS, 0, s>>>(folds, fold_blocks, leaf, n, params);
   k_morton<<<grid_for(n, BUILD_THREADS), BUILD_THREADS, 0, s>>>(leaf, n, params, keys[0]);
   const int which = radix_sort_pairs(keys, vals, n, 30, true, s, d_err);
   if(which < 0) return which;

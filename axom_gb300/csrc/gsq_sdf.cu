@@ -168,6 +168,7 @@ void sdf_release(gsq_sdf* h)
   if(h->leaves32) cudaFree(h->leaves32);
   if(h->d_audit) cudaFree(h->d_audit);
   if(h->d_work) cudaFree(h->d_work);
+  if(h->d_mesh) cudaFree(h->d_mesh);
   if(h->d_err) cudaFree(h->d_err);
   if(h->bvh) gsq_bvh_destroy(h->bvh);
   delete h;
@@ -317,6 +318,7 @@ int gsq_sdf_create(gsq_sdf** out, const double* x, const double* y, const double
   if(e == cudaSuccess) e = cudaMalloc(&h->leaves32, mixed_leaf_bytes(npc) * B->n);
   if(e == cudaSuccess) e = cudaMalloc(&h->d_audit, 4 * sizeof(unsigned long long));
   if(e == cudaSuccess) e = cudaMalloc(&h->d_work, sizeof(int));
+  if(e == cudaSuccess) e = cudaMalloc(&h->d_mesh, sizeof(MeshInfo));
   if(e != cudaSuccess) return bail(cuda_fail(e, "gsq_sdf_create: fp32 records"));
   rc = mixed_prepare(B->nodes, B->n - 1, h->leaves, B->n, npc, h->nodes32, h->leaves32, s);
   if(rc) return bail(rc);
@@ -324,6 +326,16 @@ int gsq_sdf_create(gsq_sdf** out, const double* x, const double* y, const double
   for(int d = 0; d < 6; ++d)
     if(std::fabs(h->domain[d]) < DBL_MAX) mm = std::max(mm, std::fabs(h->domain[d]));
   h->mesh_max = (float)(mm * (1.0 + 1e-6));
+  {
+    MeshInfo mi {};
+    mi.node_off = 0;
+    mi.leaf_off = 0;
+    std::memcpy(mi.domain, h->domain, sizeof(mi.domain));
+    mi.mesh_max = h->mesh_max;
+    e = cudaMemcpyAsync(h->d_mesh, &mi, sizeof(mi), cudaMemcpyHostToDevice, s);
+    if(e == cudaSuccess) e = cudaStreamSynchronize(s);
+    if(e != cudaSuccess) return bail(cuda_fail(e, "gsq_sdf_create: mesh entry"));
+  }
   if(e == cudaSuccess) e = cudaStreamSynchronize(s);
   if(e != cudaSuccess) return bail(cuda_fail(e, "gsq_sdf_create"));
   rc = check_device_error(h->d_err, s, "gsq_sdf_create");
@@ -434,7 +446,7 @@ int gsq_sdf_eval(const gsq_sdf* hc, const double* qx, const double* qy, const do
   cudaEventRecord(e0, s);
   if(mixed)
   {
-    rc = mixed_launch(h->npc, B->nodes, h->nodes32, h->leaves, h->leaves32, qp, m, order, prm, h->mesh_max,
+    rc = mixed_launch(h->npc, B->nodes, h->nodes32, h->leaves, h->leaves32, h->d_mesh, qp, m, order, prm,
                       static_cast<double*>(ob.dev), static_cast<double*>(cb.dev), static_cast<double*>(nb.dev),
                       h->d_err, audit ? h->d_audit : nullptr, h->d_work, h->opts.block_size, h->opts.queue_depth, s);
     if(rc) return rc;
@@ -564,7 +576,7 @@ int gsq_sdf_eval_noalloc(const gsq_sdf* hc, const double* qx, const double* qy, 
   prm.sign = h->sign;
   if(h->opts.precision == GSQ_PRECISION_MIXED)
   {
-    rc = mixed_launch(h->npc, B->nodes, h->nodes32, h->leaves, h->leaves32, qp, m, order, prm, h->mesh_max, out,
+    rc = mixed_launch(h->npc, B->nodes, h->nodes32, h->leaves, h->leaves32, h->d_mesh, qp, m, order, prm, out,
                       nullptr, nullptr, h->d_err, nullptr, h->d_work, h->opts.block_size, h->opts.queue_depth, s);
     if(rc) return rc;
   }

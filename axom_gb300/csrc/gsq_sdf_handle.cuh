@@ -3,7 +3,7 @@
 // gsq_sdf_adjoint.cu: gradients).
 #pragma once
 
-#include "gsq_sdf_device.cuh"
+#include "gsq_sdf_mixed.cuh"
 
 using gsq::NodeRec32;
 using gsq::NodeRec64;
@@ -27,6 +27,7 @@ struct gsq_sdf
   float mesh_max = 0.f;          // max |coordinate| of the mesh, rounded up
   unsigned long long* d_audit = nullptr;
   int* d_work = nullptr;          // work-queue counter of the persistent query kernel
+  gsq::MeshInfo* d_mesh = nullptr; // the single mesh's entry for the query kernel
   long long audit[4] = {0, 0, 0, 0};
   int* d_err = nullptr;
   float eval_ms = 0.f;
@@ -37,10 +38,11 @@ namespace gsq
 size_t mixed_leaf_bytes(int npc);
 int mixed_prepare(const NodeRec64* nodes64, int n_inner, const void* leaves64, int nleaves, int npc, NodeRec32* nodes32,
                   void* leaves32, cudaStream_t s);
+// The persistent mixed query over one mesh (meshes[0]; its node box in prm).
 int mixed_launch(int npc, const NodeRec64* nodes64, const NodeRec32* nodes32, const void* leaves64,
-                 const void* leaves32, const sdf::QueryPts& qp, int m, const int* order, const sdf::SdfParams& prm,
-                 float mesh_max, double* out, double* out_cp, double* out_n, int* err, unsigned long long* audit,
-                 int* work, int block, int depth, cudaStream_t s);
+                 const void* leaves32, const MeshInfo* meshes, const sdf::QueryPts& qp, int m, const int* order,
+                 const sdf::SdfParams& prm, double* out, double* out_cp, double* out_n, int* err,
+                 unsigned long long* audit, int* work, int block, int depth, cudaStream_t s);
 }  // namespace gsq
 
 namespace gsq

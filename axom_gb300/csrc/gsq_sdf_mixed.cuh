@@ -28,6 +28,17 @@ struct __align__(16) LeafRec32<4>
 static_assert(sizeof(LeafRec32<3>) == 48, "fp32 triangle leaf is 48 bytes");
 static_assert(sizeof(LeafRec32<4>) == 64, "fp32 quad leaf is 64 bytes");
 
+// Per-mesh entry of a query launch: where the mesh's node and leaf records
+// start in the shared arrays, its node box and coordinate bound.
+struct MeshInfo
+{
+  long long node_off;
+  long long leaf_off;
+  double domain[6];
+  float mesh_max;
+  int pad;
+};
+
 namespace sdf
 {
 // Squared point-triangle distance in FP32 by Voronoi regions (Ericson,

@@ -148,6 +148,37 @@ def mixed_queries(v: np.ndarray, f: np.ndarray, m: int, seed: int) -> np.ndarray
     return out
 
 
+def random_rotation(r: np.random.Generator) -> np.ndarray:
+    """A uniformly random rotation matrix (QR of a Gaussian matrix, sign-fixed)."""
+    q, rr = np.linalg.qr(r.normal(size=(3, 3)))
+    q *= np.sign(np.diag(rr))
+    if np.linalg.det(q) < 0:
+        q[:, 0] = -q[:, 0]
+    return q
+
+
+def batch_meshes(n: int, seed: int, levels=(2, 6), points=(1_000, 1_000_000), point_scale: float = 1.0):
+    """The batched workload: n icospheres, each at a uniformly random level in
+    ``levels`` (320..81,920 triangles for 2..6), randomly rotated, scaled in
+    [0.5, 2] and translated in [-10, 10]^3, each with a log-uniform number of
+    points in ``points`` (times ``point_scale``) uniform in its bounding box
+    expanded by 20%.  Returns (meshes [(V, F)], points [(M_k, 3)])."""
+    r = rng(seed)
+    cache = {}
+    meshes, pts = [], []
+    for k in range(n):
+        level = int(r.integers(levels[0], levels[1] + 1))
+        if level not in cache:
+            cache[level] = icosphere(level)
+        v0, f = cache[level]
+        v = (v0 @ random_rotation(r).T) * r.uniform(0.5, 2.0) + r.uniform(-10.0, 10.0, size=3)
+        lo, hi = np.log(points[0]), np.log(points[1])
+        m = max(1, int(round(np.exp(r.uniform(lo, hi)) * point_scale)))
+        meshes.append((v, f))
+        pts.append(uniform_queries(v, m, seed * 7919 + k))
+    return meshes, pts
+
+
 def uv_sphere(center=(0.0, 0.0, 0.0), radius=0.5, theta_res=25, phi_res=25):
     """UV sphere (quest/tests/quest_test_utilities.hpp:51-150), restated."""
     deg = math.pi / 180.0

@@ -38,6 +38,8 @@ LEVEL = 8
 MESH_SEED = 1234
 QUERIES = 1 << 24
 FALLBACK_HBM_GBS = 6800.0
+BATCH_MESHES = 512
+BATCH_SEED = 5
 
 
 def parse():
@@ -50,6 +52,10 @@ def parse():
     ap.add_argument("--precision", default="mixed", choices=["mixed", "fp64"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--cpu-seconds", type=float, default=10.0)
+    ap.add_argument("--batch-meshes", type=int, default=BATCH_MESHES,
+                    help="meshes of the batched-form leg (0 skips it)")
+    ap.add_argument("--batch-point-scale", type=float, default=1.0,
+                    help="scales every mesh's point count in the batched leg")
     return ap.parse_args()
 
 
@@ -171,6 +177,100 @@ def run_reference(args, world, rank):
                              "sample": f"{n} stratified points of {args.queries} per step, timed on {threads} threads"},
             "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
+
+
+def batched_leg(args, G, torch, lib, threads):
+    """The batched form: BATCH_MESHES icospheres of levels 2..6 (random rotation,
+    scale 0.5..2, translation in [-10, 10]^3), each with a log-uniform 1k..1M
+    points uniform in its 1.2x box.  A step rebuilds every tree and evaluates
+    every point: one CUDA graph launch."""
+    import oracle
+    from axom_gb300 import workloads as W
+    meshes, pts = W.batch_meshes(args.batch_meshes, BATCH_SEED, point_scale=args.batch_point_scale)
+    tris = sum(f.shape[0] for _, f in meshes)
+    flat = np.concatenate(pts)
+    m = flat.shape[0]
+    b = G.Batch(meshes, pts)
+    t0 = time.perf_counter()
+    tuned = b.tune()
+    tune_s = time.perf_counter() - t0
+    for _ in range(args.warmup):
+        b.run_device()
+    torch.cuda.synchronize()
+    launches0 = lib.gsq_kernel_launches()
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    graph_ms = []
+    ev0.record()
+    for _ in range(args.steps):
+        graph_ms.append(b.run_device())
+    ev1.record()
+    torch.cuda.synchronize()
+    ms = ev0.elapsed_time(ev1) / args.steps
+    launches = lib.gsq_kernel_launches() - launches0
+    # the build alone: the same meshes without points
+    bb = G.Batch(meshes, [p[:0] for p in pts])
+    build_ms = []
+    for i in range(args.warmup + args.steps):
+        bb.run_device()
+        if i >= args.warmup:
+            build_ms.append(bb.last_ms())
+    del bb
+    # end to end: pinned host vertices and points in, pinned host distances out
+    allv = np.concatenate([v for v, _ in meshes])
+    xyz = tuple(torch.from_numpy(np.ascontiguousarray(allv[:, k])).pin_memory() for k in range(3))
+    q_pin = torch.from_numpy(flat).pin_memory()
+    out_pin = torch.empty(m, dtype=torch.float64).pin_memory()
+    for _ in range(max(1, args.warmup)):
+        b.set_vertices(xyz)
+        b.set_points(q_pin)
+        b.run(out=out_pin)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        b.set_vertices(xyz)
+        b.set_points(q_pin)
+        b.run(out=out_pin)
+    torch.cuda.synchronize()
+    e2e_ms = (time.perf_counter() - t0) * 1000.0 / args.steps
+    # parity spot check: a few meshes against a standalone SignedDistance
+    d = out_pin.numpy()
+    parts = b.split(d)
+    exact = True
+    for k in np.linspace(0, len(meshes) - 1, 4).astype(int):
+        v, f = meshes[k]
+        ref = G.SignedDistance(v, f).compute_distances(pts[k][:20000])
+        exact &= bool(np.array_equal(ref.view(np.int64), parts[k][:20000].view(np.int64)))
+    # CPU estimate: the port builds and queries a sample of meshes on all host cores
+    port = oracle.Port()
+    sample_meshes = np.linspace(0, len(meshes) - 1, 8).astype(int)
+    cpu_build_s, cpu_tris, cpu_q_s, cpu_q = 0.0, 0, 0.0, 0
+    for k in sample_meshes:
+        v, f = meshes[k]
+        t0 = time.perf_counter()
+        h = port.sdf(v[:, 0], v[:, 1], v[:, 2], f)
+        cpu_build_s += time.perf_counter() - t0
+        cpu_tris += f.shape[0]
+        qs = pts[k][: min(pts[k].shape[0], 4000)]
+        t0 = time.perf_counter()
+        port.sdf_eval(h, qs, threads=threads)
+        cpu_q_s += time.perf_counter() - t0
+        cpu_q += qs.shape[0]
+    est_step_s = tris * cpu_build_s / cpu_tris + m * cpu_q_s / cpu_q
+    return {
+        "workload": f"batched form: {len(meshes)} icospheres (levels 2-6, {tris} triangles), {m} points "
+                    f"(log-uniform 1k-1M per mesh); a step rebuilds every tree and evaluates every point",
+        "value": m / (ms / 1000.0), "unit": UNIT, "ms_per_step": ms, "graph_ms": statistics.mean(graph_ms),
+        "build_only_ms": statistics.median(build_ms), "meshes": len(meshes), "triangles": int(tris),
+        "points": int(m), "tuned": tuned, "max_tree_depth": b.max_depth(), "tune_s": tune_s,
+        "gpu_launches": int(launches), "graph_launches_per_step": 1,
+        "e2e": {"value": m / (e2e_ms / 1000.0), "unit": UNIT, "ms_per_step": e2e_ms,
+                "h2d_bytes_per_step": 24 * m + 24 * int(allv.shape[0]), "d2h_bytes_per_step": 8 * m},
+        "spot_check_bit_exact": exact,
+        "cpu_baseline": {"value": m / est_step_s, "unit": UNIT, "cores": threads, "kind": "port",
+                         "sample": f"estimated: port build of {len(sample_meshes)} meshes ({cpu_tris} triangles, "
+                                   f"1 thread) and {cpu_q} of their points ({threads} threads), scaled to the "
+                                   f"batch's {tris} triangles and {m} points"},
+    }
 
 
 def workload_config(args, f):
@@ -295,6 +395,9 @@ def run_gsq(args, world, rank, local):
     }
     if not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline(port, v, f, q_host, args.cpu_seconds, threads)
+    if world == 1 and args.batch_meshes > 0:
+        del q_dev, out
+        line["batched"] = batched_leg(args, G, torch, lib, threads)
     print(json.dumps(line), flush=True)
     if dist is not None:
         dist.destroy_process_group()

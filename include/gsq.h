@@ -143,7 +143,7 @@ typedef struct gsq_sdf_opts {
   int32_t audit;          /* MIXED only: 1 re-checks every FP32 skip in FP64 and counts
                              violations and FP64 fallbacks (gsq_sdf_mixed_stats); slow */
   int32_t queue_depth;    /* MIXED only: FP64 refinements a lane queues before they run
-                             (1, 4 or 16; 0 = default 1) */
+                             (1, 4 or 16; 0 = default 4) */
   int32_t reserved[3];
 } gsq_sdf_opts;
 
@@ -232,6 +232,86 @@ int gsq_sdf_backward(const gsq_sdf* sdf, const double* qx, const double* qy, con
  *   [3] leaves skipped on the FP32 certificate.
  * No reference counterpart (the reference has only the FP64 form). */
 int gsq_sdf_mixed_stats(const gsq_sdf* sdf, int64_t* counters);
+
+/* ---- Batched signed distance -------------------------------------------
+ * Many independent surface meshes, each with its own set of query points of
+ * any size, evaluated together.  One run rebuilds the BVH of every mesh (a
+ * segmented build: each build kernel covers all meshes at once) and then
+ * evaluates every point against its own mesh with one persistent launch of
+ * the mixed-precision query kernel (FP32 certified traversal, FP64 refine and
+ * sign).  The whole sequence is captured once as a CUDA graph and replayed by
+ * each run.  Every mesh's distances and closest points equal gsq_sdf_eval on
+ * that mesh alone, and hence the reference's SignedDistance, bit for bit.
+ * No counterpart in the reference, which handles one mesh per object.
+ *
+ * Mesh sizes, connectivity and the number of points per mesh are fixed when
+ * the batch is created; vertex coordinates and point coordinates may change
+ * between runs (each run rebuilds the trees from the current coordinates). */
+typedef struct gsq_batch gsq_batch;
+
+typedef struct gsq_batch_opts {
+  int32_t block_size;      /* threads per block of the query kernel: 32..128, multiple of 32 (0 = 128) */
+  int32_t queue_depth;     /* FP64 refinements a lane queues: 1, 4 or 16 (0 = 4) */
+  int32_t stack_depth;     /* traversal stack entries: 32 or 64 (0 = 64, the reference's).  32
+                              needs every tree's deepest leaf at depth <= 31; a run that
+                              overflows it is repeated with 64 and the option set to 64 */
+  int32_t morton_bits;     /* bits of each point's Morton code in the processing order,
+                              1..30; with the mesh id they must fit 32 bits
+                              (0 = as many as fit) */
+  int32_t leaf_size;       /* boxes per BVH leaf.  Only 1, the reference's: larger leaves
+                              change which triangles the traversal examines and so can
+                              change pseudo-normal sums; 0 = 1 */
+  int32_t closest_points;  /* 1: runs also produce closest points (set at creation) */
+  int32_t reserved[2];
+} gsq_batch_opts;
+
+/* Fills opts with the defaults. */
+int gsq_batch_opts_init(gsq_batch_opts* opts);
+
+/* Creates a batch of nmeshes meshes.  Host arrays:
+ *   vert_offsets  nmeshes+1 int64: mesh k's vertices are [vert_offsets[k], vert_offsets[k+1])
+ *   cell_offsets  nmeshes+1 int64: mesh k's cells likewise; every mesh needs >= 2 cells
+ *   cells         cell_offsets[nmeshes] x nodes_per_cell vertex ids, local to the mesh
+ *                 (0 = the mesh's first vertex)
+ *   query_offsets nmeshes+1 int64: mesh k's points are [query_offsets[k], query_offsets[k+1])
+ * Totals: fewer than 2^30 cells and 2^30 points, at most 65536 meshes.
+ * watertight / compute_sign apply to every mesh.  Device buffers for all of it
+ * are allocated here, once.  opts nullable. */
+int gsq_batch_create(gsq_batch** out, int32_t nmeshes, const int64_t* vert_offsets, const int64_t* cell_offsets,
+                     const int32_t* cells, int32_t nodes_per_cell, const int64_t* query_offsets, int32_t watertight,
+                     int32_t compute_sign, const gsq_batch_opts* opts, void* stream);
+int gsq_batch_destroy(gsq_batch* batch);
+
+/* Vertex coordinates of all meshes (vert_offsets[nmeshes] each; host or device). */
+int gsq_batch_set_vertices(gsq_batch* batch, const double* x, const double* y, const double* z, void* stream);
+
+/* Query points of all meshes, query_offsets[nmeshes] x 3 (host or device). */
+int gsq_batch_set_points(gsq_batch* batch, const double* points, void* stream);
+
+/* Rebuilds every tree and evaluates every point: one graph launch.
+ *   out      query_offsets[nmeshes] signed distances (host or device; null keeps them
+ *            in the batch's device buffer, see gsq_batch_device_output)
+ *   closest  query_offsets[nmeshes] x 3 closest points (nullable; needs closest_points) */
+int gsq_batch_run(gsq_batch* batch, double* out, double* closest, void* stream);
+
+/* Device buffers holding the last run's distances and closest points (null if
+ * not produced); valid until the next run or destroy. */
+int gsq_batch_device_output(const gsq_batch* batch, const double** dist, const double** closest);
+
+/* Chooses block size, queue depth, stack depth and Morton width by timing the
+ * query kernel on a sample of the current points (every candidate in turn),
+ * after one build of the current meshes; the next run re-captures its graph.
+ * The chosen options are readable with gsq_batch_get_opts. */
+int gsq_batch_tune(gsq_batch* batch, void* stream);
+
+int gsq_batch_get_opts(const gsq_batch* batch, gsq_batch_opts* opts);
+/* Replaces the options (closest_points stays as created); the next run re-captures. */
+int gsq_batch_set_opts(gsq_batch* batch, const gsq_batch_opts* opts);
+
+/* Milliseconds of device time of the last run (the whole graph), and the
+ * deepest leaf over all trees as of the last tune (-1 before). */
+int gsq_batch_last_ms(const gsq_batch* batch, float* ms);
+int gsq_batch_max_depth(const gsq_batch* batch, int32_t* depth);
 
 #ifdef __cplusplus
 }

@@ -72,3 +72,33 @@ def test_opts_defaults(lib):
     o = axom_gb300.SdfOpts()
     assert lib.gsq_sdf_opts_init(C.byref(o)) == 0
     assert o.precision == 0 and o.sort_queries == 1
+
+
+def test_batch_argument_validation_without_gpu(lib):
+    import axom_gb300
+    o = axom_gb300.BatchOpts()
+    assert lib.gsq_batch_opts_init(C.byref(o)) == 0
+    h = C.c_void_p()
+    vp = lambda a: C.c_void_p(a.ctypes.data)  # noqa: E731
+    voff = np.array([0, 4, 8], np.int64)
+    coff = np.array([0, 2, 4], np.int64)
+    qoff = np.array([0, 10, 10], np.int64)
+    cells = np.zeros(12, np.int32)
+    bad_cells = np.array([0, 1, 4], np.int64)
+    assert lib.gsq_batch_create(C.byref(h), 2, vp(voff), vp(bad_cells), vp(cells), 3, vp(qoff), 1, 1, None,
+                                None) == -1
+    assert b"at least 2 cells" in lib.gsq_last_error()
+    assert lib.gsq_batch_create(C.byref(h), 0, vp(voff), vp(coff), vp(cells), 3, vp(qoff), 1, 1, None, None) == -1
+    assert lib.gsq_batch_create(C.byref(h), 2, vp(voff), vp(coff), vp(cells), 5, vp(qoff), 1, 1, None, None) == -1
+    shrinking = np.array([0, 10, 5], np.int64)
+    assert lib.gsq_batch_create(C.byref(h), 2, vp(voff), vp(coff), vp(cells), 3, vp(shrinking), 1, 1, None,
+                                None) == -1
+    o.leaf_size = 2
+    assert lib.gsq_batch_create(C.byref(h), 2, vp(voff), vp(coff), vp(cells), 3, vp(qoff), 1, 1, C.byref(o),
+                                None) == -1
+    assert b"leaf_size" in lib.gsq_last_error()
+    o.leaf_size, o.queue_depth = 1, 3
+    assert lib.gsq_batch_create(C.byref(h), 2, vp(voff), vp(coff), vp(cells), 3, vp(qoff), 1, 1, C.byref(o),
+                                None) == -1
+    assert lib.gsq_batch_run(None, None, None, None) == -1
+    assert lib.gsq_batch_destroy(None) == 0
