@@ -40,7 +40,11 @@ def standalone(meshes, pts, watertight=True, sign=True, closest=True):
     for (v, f), p in zip(meshes, pts):
         sd = axom_gb300.SignedDistance(v, f, is_watertight=watertight, compute_sign=sign,
                                        precision=axom_gb300.PRECISION_FP64)
-        res.append(sd.compute_distances(p, closest=closest) if closest else (sd.compute_distances(p), None))
+        if closest:
+            d, cp, _ = sd.compute_distances(p, closest=True)
+            res.append((d, cp))
+        else:
+            res.append((sd.compute_distances(p), None))
     return res
 
 
