@@ -116,22 +116,21 @@ __device__ __forceinline__ void qctx_init(QCtx& c, const double* q, float mesh_m
   c.lip = __fmul_ru(0x1p-21f, __fadd_ru(qabs, mesh_max));
 }
 
-// Thresholds for an exact FP64 minimum known to lie in [lo, hi].
-__device__ __forceinline__ void qctx_set(QCtx& c, double lo, double hi)
-{
-  c.t_true = __double2float_rd(lo * (1.0 - 0x1p-40));
-  c.t_false = __double2float_ru(hi * (1.0 + 0x1p-40));
-  c.thr_leaf = __fadd_ru(__double2float_ru(sqrt(hi)), 1.0001e-6f);
-}
-
-__device__ __forceinline__ void qctx_update(QCtx& c, double minSq) { qctx_set(c, minSq, minSq); }
-
-// The same from FP32 bounds lo <= minSq <= hi (no FP64 work).
+// Thresholds for an exact minimum known to lie in the FP32 interval [lo, hi]:
+// t_true <= minSq (1 - 2^-40) and t_false >= minSq (1 + 2^-40) with room for
+// the FP64 predicate's own rounding; thr_leaf >= sqrt(minSq) + 1e-6.  No FP64
+// arithmetic.
 __device__ __forceinline__ void qctx_set32(QCtx& c, float lo, float hi)
 {
   c.t_true = __fmul_rd(lo, 1.f - 0x1p-22f);
   c.t_false = __fmul_ru(hi, 1.f + 0x1p-22f);
   c.thr_leaf = __fadd_ru(__fsqrt_ru(hi), 1.0001e-6f);
+}
+
+// The same for an exactly known FP64 minimum.
+__device__ __forceinline__ void qctx_update(QCtx& c, double minSq)
+{
+  qctx_set32(c, __double2float_rd(minSq), __double2float_ru(minSq));
 }
 
 // squared_distance(p, box) <= minSq decided in FP32 (SD:576-578).  s is the

@@ -110,9 +110,11 @@ __global__ void __launch_bounds__(128, 5) k_sdf_mixed(const NodeRec64* __restric
     qctx_set32(c, fminf(reset ? INFINITY : mlo, plo), fminf(reset ? INFINITY : mhi, phi));
   };
   auto resolved = [&]() {
-    qctx_update(c, mc.minSq);
+    // thresholds from the FP32 enclosure of the exact minimum (no FP64 math:
+    // FP64 instructions are the scarcest resource of this GPU)
     mlo = __double2float_rd(mc.minSq);
     mhi = __double2float_ru(mc.minSq);
+    qctx_set32(c, mlo, mhi);
     mvalid = mc.minSq < DBL_MAX;
     for(int d = 0; d < 3; ++d) mpf[d] = (float)mc.mp[d];
     reset = false;
