@@ -39,6 +39,10 @@ MESH_SEED = 1234
 QUERIES = 1 << 24
 FALLBACK_HBM_GBS = 6800.0
 BATCH_MESHES = 512
+# DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) per point of one
+# k_sdf_mixed launch, measured by ncu on 1,048,576 uniform points of the same
+# mesh (1.936 GB read + 0.522 GB written); the bench scales it by its point count.
+MIXED_DRAM_BYTES_PER_POINT = (1.936470e9 + 0.522434e9) / 1048576
 BATCH_SEED = 5
 
 
@@ -52,6 +56,8 @@ def parse():
     ap.add_argument("--precision", default="mixed", choices=["mixed", "fp64"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--cpu-seconds", type=float, default=10.0)
+    ap.add_argument("--no-forms", dest="forms", action="store_false",
+                    help="skip the near-surface and adjoint legs")
     ap.add_argument("--batch-meshes", type=int, default=BATCH_MESHES,
                     help="meshes of the batched-form leg (0 skips it)")
     ap.add_argument("--batch-point-scale", type=float, default=1.0,
@@ -273,6 +279,70 @@ def batched_leg(args, G, torch, lib, threads):
     }
 
 
+def near_surface_leg(args, G, torch, v, f):
+    """Sign robustness at scale: 16M points on the level-8 mesh, half uniform in
+    the 1.2x box and half at a random surface point offset along the normal by
+    10^U[-9,-3] (either side).  The mixed form against the FP64 form on the
+    GPU over every point: relative error and sign mismatches."""
+    from axom_gb300 import workloads as W
+    m = args.queries
+    q = torch.from_numpy(W.mixed_queries(v, f, m, 4)).cuda()
+    sd = G.SignedDistance(v, f, precision=G.PRECISION_MIXED)
+    dm = torch.empty(m, dtype=torch.float64, device="cuda")
+    for _ in range(args.warmup):
+        sd.compute_distances(q, out=dm)
+    kms = []
+    for _ in range(args.steps):
+        sd.compute_distances(q, out=dm)
+        kms.append(sd.last_eval_ms())
+    sd.set_precision(G.PRECISION_FP64)
+    d64 = sd.compute_distances(q)
+    rel = (dm - d64).abs() / d64.abs().clamp_min(1e-300)
+    res = {"workload": f"{m} points: half uniform in the 1.2x box, half within 1e-9..1e-3 of the surface",
+           "value": m / (statistics.median(kms) / 1000.0), "unit": UNIT, "kernel_ms": statistics.median(kms),
+           "fp64_kernel_ms": sd.last_eval_ms(),
+           "sign_mismatches": int((torch.signbit(dm) != torch.signbit(d64)).sum().item()),
+           "max_rel_err": float(rel.max().item()),
+           "rel_err_p50_p99_p999": [float(x) for x in torch.quantile(
+               rel[:: max(1, m // (1 << 20))].float(), torch.tensor([0.5, 0.99, 0.999], device="cuda")).tolist()],
+           "bit_identical_to_fp64": bool(torch.equal(dm.view(torch.int64), d64.view(torch.int64)))}
+    del q, dm, d64
+    return res
+
+
+def adjoint_leg(args, G, torch):
+    """Differentiated form: level-6 displaced icosphere (81,920 triangles),
+    1,048,576 uniform points, L = sum w d^2 with w ~ U[0,1]: forward (mixed)
+    plus the hand-written adjoint (dL/dpoints and the deterministic vertex
+    reduction) per step."""
+    from axom_gb300 import workloads as W
+    v, f = W.displaced_icosphere(6, MESH_SEED)
+    m = 1 << 20
+    q = torch.from_numpy(W.uniform_queries(v, m, 3)).cuda()
+    w = torch.from_numpy(np.random.default_rng(6).uniform(0, 1, m)).cuda()
+    sd = G.SignedDistance(v, f, precision=G.PRECISION_MIXED)
+
+    def step():
+        d = sd.compute_distances(q)
+        return sd.backward(q, 2.0 * w * d)
+
+    for _ in range(args.warmup):
+        step()
+    torch.cuda.synchronize()
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    ev0.record()
+    for _ in range(args.steps):
+        gp, gv = step()
+    ev1.record()
+    torch.cuda.synchronize()
+    ms = ev0.elapsed_time(ev1) / args.steps
+    gp2, gv2 = step()
+    return {"workload": f"level-6 mesh ({f.shape[0]} triangles, {v.shape[0]} vertices), {m} uniform points, "
+                        "forward + backward per step",
+            "value": m / (ms / 1000.0), "unit": "points/s (forward + backward)", "ms_per_step": ms,
+            "deterministic": bool(torch.equal(gv.view(torch.int64), gv2.view(torch.int64)))}
+
+
 def workload_config(args, f):
     return {"workload": f"signed distance: displaced icosphere level {LEVEL} ({f.shape[0]} triangles), "
                         f"{args.queries} uniform points in the 1.2x box per GPU",
@@ -384,7 +454,9 @@ def run_gsq(args, world, rank, local):
         "fp64": fp64,
         "build_ms": {"value": statistics.median(build_ms), "boxes": int(f.shape[0]), "runs": len(build_ms)},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
-                     "traffic": None, "peak_kind": hbm_kind,
+                     "traffic": MIXED_DRAM_BYTES_PER_POINT * m if args.precision == "mixed" else None,
+                     "traffic_note": "ncu DRAM bytes per point on a 1,048,576-point launch, scaled to this launch",
+                     "peak_kind": hbm_kind,
                      "kernel": "k_sdf_mixed" if args.precision == "mixed" else "k_sdf_fp64",
                      "kernel_ms": kernel_ms,
                      "algorithmic_bytes_per_query": bq, "box_tests_per_query": nb, "leaf_tests_per_query": nl},
@@ -395,8 +467,11 @@ def run_gsq(args, world, rank, local):
     }
     if not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline(port, v, f, q_host, args.cpu_seconds, threads)
+    if world == 1 and args.forms:
+        line["near_surface"] = near_surface_leg(args, G, torch, v, f)
+        line["adjoint"] = adjoint_leg(args, G, torch)
     if world == 1 and args.batch_meshes > 0:
-        del q_dev, out
+        torch.cuda.empty_cache()
         line["batched"] = batched_leg(args, G, torch, lib, threads)
     print(json.dumps(line), flush=True)
     if dist is not None:
