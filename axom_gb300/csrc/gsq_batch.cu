@@ -551,6 +551,8 @@ int gsq_batch_create(gsq_batch** out, int32_t nmeshes, const int64_t* vert_offse
   if(!valid_offsets(vert_offsets, nmeshes, false) || !valid_offsets(query_offsets, nmeshes, false))
     return fail(GSQ_ERR_INVALID, "offsets must start at 0 and not decrease");
   if(!valid_offsets(cell_offsets, nmeshes, true)) return fail(GSQ_ERR_INVALID, "every mesh needs at least 2 cells");
+  for(int k = 0; k < nmeshes; ++k)
+    if(cell_offsets[k + 1] - cell_offsets[k] >= (1 << 28)) return fail(GSQ_ERR_INVALID, "at most 2^28-1 cells per mesh");
   const long long V = vert_offsets[nmeshes], Cn = cell_offsets[nmeshes], M = query_offsets[nmeshes];
   if(Cn >= (1LL << 30) || M >= (1LL << 30) || V >= (1LL << 31) - 1)
     return fail(GSQ_ERR_INVALID, "batch too large (cells and points < 2^30, vertices < 2^31)");

@@ -247,7 +247,7 @@ int gsq_sdf_create(gsq_sdf** out, const double* x, const double* y, const double
   *out = nullptr;
   if(nverts < 0 || ncells < 0 || (npc != 3 && npc != 4)) return fail(GSQ_ERR_INVALID, "invalid mesh sizes");
   if((nverts > 0 && (!x || !y || !z)) || (ncells > 0 && !cells)) return fail(GSQ_ERR_INVALID, "null mesh arrays");
-  if(ncells >= (1 << 30)) return fail(GSQ_ERR_INVALID, "at most 2^30-1 cells");
+  if(ncells >= (1 << 28)) return fail(GSQ_ERR_INVALID, "at most 2^28-1 cells");
   cudaStream_t s = static_cast<cudaStream_t>(stream);
   auto* h = new(std::nothrow) gsq_sdf();
   if(!h) return fail(GSQ_ERR_NOMEM, "handle allocation failed");

@@ -115,6 +115,12 @@ __device__ __forceinline__ double query_sign(const double* q, const MinCand& mc,
     else
       tri_normal(v, v + 3, v + 6, nrm);
   }
+  else if(mc.npend > 0)
+  {
+    MinCand m = mc;
+    flush_normals<NPC>(m, leaves);
+    nrm[0] = m.sn[0], nrm[1] = m.sn[1], nrm[2] = m.sn[2];
+  }
   const double r0 = q[0] - mc.mp[0], r1 = q[1] - mc.mp[1], r2 = q[2] - mc.mp[2];
   return (dot3(r0, r1, r2, nrm[0], nrm[1], nrm[2]) >= 0.0) ? 1.0 : -1.0;
 }

@@ -149,19 +149,81 @@ __device__ __forceinline__ bool tri_degenerate(const double* A, const double* B,
 
 // MinCandidate (SD:159-175); the closest element's geometry is kept as its
 // leaf position and sub-triangle and reloaded at the end.
+//
+// The pseudo-normal sum is accumulated lazily: checkCandidate's contributions
+// (SD:709-736) are recorded in order and only evaluated when the sum is needed
+// (flush_normals) or the list is full.  A clear (a strictly closer point that
+// is not the same shared vertex or edge) drops the list unevaluated.  The sum
+// is formed from the same terms in the same order, so it equals the eager
+// sum bit for bit; most contributions of far points are cleared later, and
+// each costs a normal, a square root and (for vertices) an arccosine in FP64.
+constexpr int NPEND = 8;
 struct MinCand
 {
   double minSq;
   double mp[3];
-  double sn[3];
-  int type;  // -1 uninitialized, 0 vertex, 1 edge, 2 face (SD:110-137)
+  double sn[3];  // the sum of the contributions evaluated so far
+  int type;      // -1 uninitialized, 0 vertex, 1 edge, 2 face (SD:110-137)
   int leaf;
   int sub;
+  int npend;           // contributions recorded after those in sn
+  int pend[NPEND];     // leafpos * 8 + sub * 4 + (vertex index 0..2, or 3 for an edge)
 };
 
-// checkCandidate for one triangle (SD:667-736)
-__device__ __forceinline__ void check_triangle(const double* q, MinCand& m, const double* const* T, int leafpos,
-                                               int sub, bool computeNormal)
+template <int NPC>
+__device__ __forceinline__ void load_leaf(const LeafRec<NPC>* __restrict__ leaves, int leafpos, double* v)
+{
+  const double2* r = reinterpret_cast<const double2*>(leaves + leafpos);
+#pragma unroll
+  for(int k = 0; k < (3 * NPC) / 2; ++k)
+  {
+    const double2 t = __ldg(r + k);
+    v[2 * k] = t.x;
+    v[2 * k + 1] = t.y;
+  }
+  if((3 * NPC) % 2) v[3 * NPC - 1] = __ldg(&leaves[leafpos].v[3 * NPC - 1]);
+}
+
+// One recorded contribution to the pseudo-normal sum (SD:709-736).
+template <int NPC>
+__device__ __forceinline__ void add_normal(MinCand& m, const LeafRec<NPC>* __restrict__ leaves, int code)
+{
+  double v[3 * NPC];
+  load_leaf<NPC>(leaves, code >> 3, v);
+  const int s = (code >> 2) & 1;
+  const double* T[3] = {v, v + 3 * (s + 1), v + 3 * (s + 2)};
+  const int k = code & 3;
+  if(k == 3)
+  {
+    double n[3], u[3];
+    tri_normal(T[0], T[1], T[2], n);
+    unit3(n, u);
+    m.sn[0] = m.sn[0] + u[0], m.sn[1] = m.sn[1] + u[1], m.sn[2] = m.sn[2] + u[2];
+  }
+  else if(!tri_degenerate(T[0], T[1], T[2]))
+  {
+    const double alpha = tri_angle(T, k);
+    double n[3], u[3];
+    tri_normal(T[0], T[1], T[2], n);
+    unit3(n, u);
+    m.sn[0] = m.sn[0] + u[0] * alpha, m.sn[1] = m.sn[1] + u[1] * alpha, m.sn[2] = m.sn[2] + u[2] * alpha;
+  }
+}
+
+// Evaluates the recorded contributions into sn, in order.
+template <int NPC>
+__device__ __forceinline__ void flush_normals(MinCand& m, const LeafRec<NPC>* __restrict__ leaves)
+{
+  for(int i = 0; i < m.npend; ++i) add_normal<NPC>(m, leaves, m.pend[i]);
+  m.npend = 0;
+}
+
+// checkCandidate for one triangle (SD:667-736); sub-triangle `sub` of leaf
+// `leafpos` with vertices T.
+template <int NPC>
+__device__ __forceinline__ void check_triangle(const double* q, MinCand& m, const double* const* T,
+                                               const LeafRec<NPC>* __restrict__ leaves, int leafpos, int sub,
+                                               bool computeNormal)
 {
   double cp[3];
   const int loc = closest_point(q, T[0], T[1], T[2], cp);
@@ -177,43 +239,20 @@ __device__ __forceinline__ void check_triangle(const double* q, MinCand& m, cons
     m.type = ty;
     m.leaf = leafpos;
     m.sub = sub;
-    if(computeNormal && clear) m.sn[0] = m.sn[1] = m.sn[2] = 0.0;
+    if(computeNormal && clear)
+    {
+      m.sn[0] = m.sn[1] = m.sn[2] = 0.0;
+      m.npend = 0;
+    }
     upd = computeNormal && shared;
   }
   else
     upd = computeNormal && shared && (m.type == ty) && near_eq(sqdist_pp(cp, m.mp), 0.0, CP_EPS);
   if(upd)
   {
-    if(ty == 1)
-    {
-      double n[3], u[3];
-      tri_normal(T[0], T[1], T[2], n);
-      unit3(n, u);
-      m.sn[0] = m.sn[0] + u[0], m.sn[1] = m.sn[1] + u[1], m.sn[2] = m.sn[2] + u[2];
-    }
-    else if(!tri_degenerate(T[0], T[1], T[2]))
-    {
-      const double alpha = tri_angle(T, loc);
-      double n[3], u[3];
-      tri_normal(T[0], T[1], T[2], n);
-      unit3(n, u);
-      m.sn[0] = m.sn[0] + u[0] * alpha, m.sn[1] = m.sn[1] + u[1] * alpha, m.sn[2] = m.sn[2] + u[2] * alpha;
-    }
+    if(m.npend == NPEND) flush_normals<NPC>(m, leaves);
+    m.pend[m.npend++] = leafpos * 8 + sub * 4 + (ty == 1 ? 3 : loc);
   }
-}
-
-template <int NPC>
-__device__ __forceinline__ void load_leaf(const LeafRec<NPC>* __restrict__ leaves, int leafpos, double* v)
-{
-  const double2* r = reinterpret_cast<const double2*>(leaves + leafpos);
-#pragma unroll
-  for(int k = 0; k < (3 * NPC) / 2; ++k)
-  {
-    const double2 t = __ldg(r + k);
-    v[2 * k] = t.x;
-    v[2 * k + 1] = t.y;
-  }
-  if((3 * NPC) % 2) v[3 * NPC - 1] = __ldg(&leaves[leafpos].v[3 * NPC - 1]);
 }
 
 // squared_distance(Point, BoundingBox) (squared_distance.hpp:77-102)
@@ -249,6 +288,7 @@ __device__ __forceinline__ void init_min(MinCand& mc)
   mc.type = -1;
   mc.leaf = -1;
   mc.sub = 0;
+  mc.npend = 0;
 }
 
 // Sign (SD:583-592) and outputs (SD:594-603) of one query.
@@ -257,8 +297,13 @@ __device__ __forceinline__ void finish_query(const double* q, const MinCand& mc,
                                              const SdfParams& prm, int idx, double* __restrict__ out,
                                              double* __restrict__ out_cp, double* __restrict__ out_n)
 {
-  // getSurfaceNormal (SD:740-748)
+  // getSurfaceNormal (SD:740-748); the recorded pseudo-normal terms are
+  // evaluated only when the normal is used
   double nrm[3] = {mc.sn[0], mc.sn[1], mc.sn[2]};
+  const double* D = prm.domain;
+  const bool inside_box = !(mc.mp[0] < D[0] || mc.mp[0] > D[3] || mc.mp[1] < D[1] || mc.mp[1] > D[4] ||
+                            mc.mp[2] < D[2] || mc.mp[2] > D[5]);
+  const bool want_sign = prm.sign && !(prm.watertight && !inside_box);
   if(mc.type == 2)
   {
     double v[3 * NPC];
@@ -268,18 +313,18 @@ __device__ __forceinline__ void finish_query(const double* q, const MinCand& mc,
     else
       tri_normal(v, v + 3, v + 6, nrm);
   }
-  double sgn = 1.0;
-  if(prm.sign)
+  else if(mc.npend > 0 && (want_sign || out_n))
   {
-    const double* D = prm.domain;
-    const bool inside_box = !(mc.mp[0] < D[0] || mc.mp[0] > D[3] || mc.mp[1] < D[1] || mc.mp[1] > D[4] ||
-                              mc.mp[2] < D[2] || mc.mp[2] > D[5]);
-    if(!(prm.watertight && !inside_box))
-    {
-      // computeSign (SD:751-763)
-      const double r0 = q[0] - mc.mp[0], r1 = q[1] - mc.mp[1], r2 = q[2] - mc.mp[2];
-      sgn = (dot3(r0, r1, r2, nrm[0], nrm[1], nrm[2]) >= 0.0) ? 1.0 : -1.0;
-    }
+    MinCand m = mc;
+    flush_normals<NPC>(m, leaves);
+    nrm[0] = m.sn[0], nrm[1] = m.sn[1], nrm[2] = m.sn[2];
+  }
+  double sgn = 1.0;
+  if(want_sign)
+  {
+    // computeSign (SD:751-763)
+    const double r0 = q[0] - mc.mp[0], r1 = q[1] - mc.mp[1], r2 = q[2] - mc.mp[2];
+    sgn = (dot3(r0, r1, r2, nrm[0], nrm[1], nrm[2]) >= 0.0) ? 1.0 : -1.0;
   }
   out[idx] = sqrt(mc.minSq) * sgn;
   if(out_cp)
@@ -307,11 +352,11 @@ __device__ __forceinline__ void check_leaf(const double* q, MinCand& mc, const L
   double v[3 * NPC];
   load_leaf<NPC>(leaves, leafpos, v);
   const double* T0[3] = {v, v + 3, v + 6};
-  check_triangle(q, mc, T0, leafpos, 0, computeNormal);
+  check_triangle<NPC>(q, mc, T0, leaves, leafpos, 0, computeNormal);
   if constexpr(NPC == 4)
   {
     const double* T1[3] = {v, v + 6, v + 9};
-    check_triangle(q, mc, T1, leafpos, 1, computeNormal);
+    check_triangle<NPC>(q, mc, T1, leaves, leafpos, 1, computeNormal);
   }
 }
 

@@ -328,6 +328,16 @@ __device__ __forceinline__ int leaf_audit(const LeafRec<NPC>* __restrict__ leave
   return bad;
 }
 
+// Audit: two checkCandidate states are the same (pseudo-normal sums evaluated).
+template <int NPC>
+__device__ __forceinline__ bool same_state(MinCand a, MinCand b, const LeafRec<NPC>* __restrict__ leaves64)
+{
+  flush_normals<NPC>(a, leaves64);
+  flush_normals<NPC>(b, leaves64);
+  return a.minSq == b.minSq && a.type == b.type && a.leaf == b.leaf && a.sub == b.sub && a.mp[0] == b.mp[0] &&
+         a.mp[1] == b.mp[1] && a.mp[2] == b.mp[2] && a.sn[0] == b.sn[0] && a.sn[1] == b.sn[1] && a.sn[2] == b.sn[2];
+}
+
 // FP64 checkCandidate on the triangles of `need`, in the reference's order.
 template <int NPC>
 __device__ __forceinline__ void leaf_refine(const LeafRec<NPC>* __restrict__ leaves64, int leafpos, int need,
@@ -340,7 +350,7 @@ __device__ __forceinline__ void leaf_refine(const LeafRec<NPC>* __restrict__ lea
   {
     if(!(need & (1 << s))) continue;
     const double* T[3] = {w, w + 3 * (s + 1), w + 3 * (s + 2)};
-    check_triangle(q, mc, T, leafpos, s, computeNormal);
+    check_triangle<NPC>(q, mc, T, leaves64, leafpos, s, computeNormal);
   }
 }
 

@@ -303,11 +303,7 @@ __global__ void __launch_bounds__(128, 5) k_sdf_mixed(const NodeRec64* __restric
               for(int j = 0; j < np; ++j) leaf_refine<NPC>(leaves64, pq[j] >> 2, pq[j] & 3, q, s1, computeNormal);
               MinCand s2 = s1;
               leaf_refine<NPC>(leaves64, lp, need, q, s2, computeNormal);
-              const bool same = s1.minSq == s2.minSq && s1.type == s2.type && s1.leaf == s2.leaf &&
-                                s1.sub == s2.sub && s1.mp[0] == s2.mp[0] && s1.mp[1] == s2.mp[1] &&
-                                s1.mp[2] == s2.mp[2] && s1.sn[0] == s2.sn[0] && s1.sn[1] == s2.sn[1] &&
-                                s1.sn[2] == s2.sn[2];
-              if(!same) ++st[0];
+              if(!same_state<NPC>(s1, s2, leaves64)) ++st[0];
             }
           }
           if(noop)
@@ -331,11 +327,7 @@ __global__ void __launch_bounds__(128, 5) k_sdf_mixed(const NodeRec64* __restric
                 leaf_refine<NPC>(leaves64, lp, need, q, s1, computeNormal);
                 init_min(s2);
                 leaf_refine<NPC>(leaves64, lp, need, q, s2, computeNormal);
-                const bool same = s1.minSq == s2.minSq && s1.type == s2.type && s1.leaf == s2.leaf &&
-                                  s1.sub == s2.sub && s1.mp[0] == s2.mp[0] && s1.mp[1] == s2.mp[1] &&
-                                  s1.mp[2] == s2.mp[2] && s1.sn[0] == s2.sn[0] && s1.sn[1] == s2.sn[1] &&
-                                  s1.sn[2] == s2.sn[2];
-                if(!same) ++st[0];
+                if(!same_state<NPC>(s1, s2, leaves64)) ++st[0];
               }
               np = 0;
               plo = phi = INFINITY;

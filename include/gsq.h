@@ -154,7 +154,7 @@ int gsq_sdf_opts_init(gsq_sdf_opts* opts);
  * and setMesh (quest/SignedDistance.hpp:410-504): mesh box, per-cell boxes
  * and the BVH build.  The mesh is an unstructured single-shape surface mesh:
  *   x, y, z         : nverts node coordinates
- *   cells           : ncells x nodes_per_cell node ids (int32)
+ *   cells           : ncells x nodes_per_cell node ids (int32), ncells < 2^28
  *   nodes_per_cell  : 3 (triangles) or 4 (quads, split as the reference does)
  * The handle keeps its own device copy of the mesh (the reference borrows
  * the mint mesh).  opts nullable. */
@@ -274,7 +274,8 @@ int gsq_batch_opts_init(gsq_batch_opts* opts);
  *   cells         cell_offsets[nmeshes] x nodes_per_cell vertex ids, local to the mesh
  *                 (0 = the mesh's first vertex)
  *   query_offsets nmeshes+1 int64: mesh k's points are [query_offsets[k], query_offsets[k+1])
- * Totals: fewer than 2^30 cells and 2^30 points, at most 65536 meshes.
+ * Totals: fewer than 2^30 cells and 2^30 points, at most 65536 meshes, fewer
+ * than 2^28 cells per mesh.
  * watertight / compute_sign apply to every mesh.  Device buffers for all of it
  * are allocated here, once.  opts nullable. */
 int gsq_batch_create(gsq_batch** out, int32_t nmeshes, const int64_t* vert_offsets, const int64_t* cell_offsets,
