@@ -39,6 +39,12 @@ __device__ __forceinline__ double sqdist_pp(const double* a, const double* b)
 
 __device__ __forceinline__ bool is_leq(double x, double y) { return !((x > y) && !near_eq(x, y, CP_EPS)); }
 __device__ __forceinline__ bool is_geq(double x, double y) { return !((x < y) && !near_eq(x, y, CP_EPS)); }
+// The same predicates in one comparison, given d = x - y rounded: x > y makes
+// the rounded difference positive (FP64 keeps subnormals), so "x > y and
+// |x - y| > EPS" is "d > EPS", and "x < y and |x - y| > EPS" is "d < -EPS";
+// NaNs give true as in is_leq/is_geq.  For y = 0, d is x itself.
+__device__ __forceinline__ bool leq_d(double d) { return !(d > CP_EPS); }
+__device__ __forceinline__ bool geq_d(double d) { return !(d < -CP_EPS); }
 
 // closest_point(Point, Triangle, loc, EPS) (primal/operators/closest_point.hpp:162-290)
 __device__ __forceinline__ int closest_point(const double* P, const double* A, const double* B, const double* C,
@@ -49,7 +55,7 @@ __device__ __forceinline__ int closest_point(const double* P, const double* A, c
   const double ap0 = P[0] - A[0], ap1 = P[1] - A[1], ap2 = P[2] - A[2];
   const double d1 = dot3(ab0, ab1, ab2, ap0, ap1, ap2);
   const double d2 = dot3(ac0, ac1, ac2, ap0, ap1, ap2);
-  if(is_leq(d1, 0.0) && is_leq(d2, 0.0))
+  if(leq_d(d1) && leq_d(d2))  // is_leq(d1, 0) && is_leq(d2, 0)
   {
     out[0] = A[0], out[1] = A[1], out[2] = A[2];
     return 0;
@@ -57,13 +63,13 @@ __device__ __forceinline__ int closest_point(const double* P, const double* A, c
   const double bp0 = P[0] - B[0], bp1 = P[1] - B[1], bp2 = P[2] - B[2];
   const double d3 = dot3(ab0, ab1, ab2, bp0, bp1, bp2);
   const double d4 = dot3(ac0, ac1, ac2, bp0, bp1, bp2);
-  if(is_geq(d3, 0.0) && is_leq(d4, d3))
+  if(geq_d(d3) && leq_d(d4 - d3))  // is_geq(d3, 0) && is_leq(d4, d3)
   {
     out[0] = B[0], out[1] = B[1], out[2] = B[2];
     return 1;
   }
   const double vc = d1 * d4 - d3 * d2;
-  if(is_leq(vc, 0.0) && is_geq(d1, 0.0) && is_leq(d3, 0.0) && !near_eq(d1, d3, CP_EPS))
+  if(leq_d(vc) && geq_d(d1) && leq_d(d3) && !near_eq(d1, d3, CP_EPS))
   {
     const double v = d1 / (d1 - d3);
     out[0] = A[0] + ab0 * v, out[1] = A[1] + ab1 * v, out[2] = A[2] + ab2 * v;
@@ -72,20 +78,20 @@ __device__ __forceinline__ int closest_point(const double* P, const double* A, c
   const double cp0 = P[0] - C[0], cp1 = P[1] - C[1], cp2 = P[2] - C[2];
   const double d5 = dot3(ab0, ab1, ab2, cp0, cp1, cp2);
   const double d6 = dot3(ac0, ac1, ac2, cp0, cp1, cp2);
-  if(is_geq(d6, 0.0) && is_leq(d5, d6))
+  if(geq_d(d6) && leq_d(d5 - d6))  // is_geq(d6, 0) && is_leq(d5, d6)
   {
     out[0] = C[0], out[1] = C[1], out[2] = C[2];
     return 2;
   }
   const double vb = d5 * d2 - d1 * d6;
-  if(is_leq(vb, 0.0) && is_geq(d2, 0.0) && is_leq(d6, 0.0))
+  if(leq_d(vb) && geq_d(d2) && leq_d(d6))
   {
     const double w = d2 / (d2 - d6);
     out[0] = A[0] + ac0 * w, out[1] = A[1] + ac1 * w, out[2] = A[2] + ac2 * w;
     return -3;
   }
   const double va = d3 * d6 - d5 * d4;
-  if(is_leq(va, 0.0) && is_geq(d4 - d3, 0.0) && is_geq(d5 - d6, 0.0))
+  if(leq_d(va) && geq_d(d4 - d3) && geq_d(d5 - d6))
   {
     const double w = (d4 - d3) / ((d4 - d3) + (d5 - d6));
     out[0] = B[0] + (C[0] - B[0]) * w, out[1] = B[1] + (C[1] - B[1]) * w, out[2] = B[2] + (C[2] - B[2]) * w;
@@ -218,16 +224,14 @@ __device__ __forceinline__ void flush_normals(MinCand& m, const LeafRec<NPC>* __
   m.npend = 0;
 }
 
-// checkCandidate for one triangle (SD:667-736); sub-triangle `sub` of leaf
-// `leafpos` with vertices T.
+// checkCandidate's state update (SD:675-736) for a triangle whose closest
+// point cp (location loc, squared distance sq) is already known; sub-triangle
+// `sub` of leaf `leafpos`.
 template <int NPC>
-__device__ __forceinline__ void check_triangle(const double* q, MinCand& m, const double* const* T,
-                                               const LeafRec<NPC>* __restrict__ leaves, int leafpos, int sub,
-                                               bool computeNormal)
+__device__ __forceinline__ void apply_candidate(const double* cp, double sq, int loc, MinCand& m,
+                                                const LeafRec<NPC>* __restrict__ leaves, int leafpos, int sub,
+                                                bool computeNormal)
 {
-  double cp[3];
-  const int loc = closest_point(q, T[0], T[1], T[2], cp);
-  const double sq = sqdist_pp(q, cp);
   const int ty = (loc < 0) ? 1 : (loc <= 2) ? 0 : 2;
   const bool shared = (ty != 2);
   bool upd;
@@ -253,6 +257,18 @@ __device__ __forceinline__ void check_triangle(const double* q, MinCand& m, cons
     if(m.npend == NPEND) flush_normals<NPC>(m, leaves);
     m.pend[m.npend++] = leafpos * 8 + sub * 4 + (ty == 1 ? 3 : loc);
   }
+}
+
+// checkCandidate for one triangle (SD:667-736); sub-triangle `sub` of leaf
+// `leafpos` with vertices T.
+template <int NPC>
+__device__ __forceinline__ void check_triangle(const double* q, MinCand& m, const double* const* T,
+                                               const LeafRec<NPC>* __restrict__ leaves, int leafpos, int sub,
+                                               bool computeNormal)
+{
+  double cp[3];
+  const int loc = closest_point(q, T[0], T[1], T[2], cp);
+  apply_candidate<NPC>(cp, sqdist_pp(q, cp), loc, m, leaves, leafpos, sub, computeNormal);
 }
 
 // squared_distance(Point, BoundingBox) (squared_distance.hpp:77-102)

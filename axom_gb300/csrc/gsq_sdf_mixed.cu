@@ -72,7 +72,12 @@ __global__ void k_nodes32(const NodeRec64* __restrict__ in, int n_inner, NodeRec
   out[i] = r;
 }
 
-__device__ __forceinline__ void tri_error_terms(const double* A, const double* B, const double* C, float& ec, float& lt)
+// Per triangle: ec = 256 * 2^-24 * kappa (kappa = L^2 / |n|, L the longest
+// edge), lt = L, and fz = 2e-12 (kappa / L + kappa^2 / L^3), the bound on how
+// far the reference's fuzzy region tests move its closest point; all rounded
+// up with a margin.
+__device__ __forceinline__ void tri_error_terms(const double* A, const double* B, const double* C, float& ec, float& lt,
+                                                float* fz = nullptr)
 {
   const double ab[3] = {B[0] - A[0], B[1] - A[1], B[2] - A[2]};
   const double ac[3] = {C[0] - A[0], C[1] - A[1], C[2] - A[2]};
@@ -85,6 +90,12 @@ __device__ __forceinline__ void tri_error_terms(const double* A, const double* B
   const double kappa = (nn > 0.0 && nn == nn) ? (L * L) / nn : INFINITY;
   ec = __double2float_ru(256.0 * 0x1p-24 * kappa * 1.01);
   lt = __double2float_ru(L * 1.0001);
+  if(fz)
+  {
+    const double kl = kappa / L;
+    const double f = 2e-12 * (kl + kl * kappa / (L * L)) * 1.03;
+    *fz = (f == f) ? __double2float_ru(f) : INFINITY;
+  }
 }
 
 template <int NPC>
@@ -97,8 +108,7 @@ __global__ void k_leaves32(const LeafRec<NPC>* __restrict__ in, int n, LeafRec32
   for(int j = 0; j < 3 * NPC; ++j) r.v[j] = (float)v[j];
   if constexpr(NPC == 3)
   {
-    tri_error_terms(v, v + 3, v + 6, r.ec, r.lt);
-    r.pad = 0.f;
+    tri_error_terms(v, v + 3, v + 6, r.ec, r.lt, &r.fz);
   }
   else
   {

@@ -9,14 +9,16 @@ namespace gsq
 template <int NPC>
 struct LeafRec32;
 // FP32 triangle(s) of one leaf: vertices rounded to nearest, and per
-// triangle the error factor ec = 256 * 2^-24 * kappa and max edge length lt.
+// triangle the error factor ec = 256 * 2^-24 * kappa and max edge length lt
+// (triangles also carry fz, the bound on the reference's fuzzy closest-point
+// displacement; quads compute it from ec and lt).
 template <>
 struct __align__(16) LeafRec32<3>
 {
   float v[9];
   float ec;
   float lt;
-  float pad;
+  float fz;
 };
 template <>
 struct __align__(16) LeafRec32<4>
@@ -43,41 +45,47 @@ namespace sdf
 {
 // Squared point-triangle distance in FP32 by Voronoi regions (Ericson,
 // Real-Time Collision Detection 5.1.5), measured from P.  off (optional)
-// receives P - cp, the offset from the closest point.
+// receives P - cp, the offset from the closest point.  Products are fused
+// (one rounding per multiply-add): the error bounds used with this function
+// count at least one rounding per operation, which fused operations meet.
+__device__ __forceinline__ float dot3f(float a0, float b0, float a1, float b1, float a2, float b2)
+{
+  return __fmaf_rn(a2, b2, __fmaf_rn(a1, b1, a0 * b0));
+}
 __device__ __forceinline__ float dist2_f32(const float* P, const float* A, const float* B, const float* C,
                                           float* off = nullptr)
 {
   auto ret = [&](float x, float y, float z) {
     if(off) off[0] = x, off[1] = y, off[2] = z;
-    return x * x + y * y + z * z;
+    return dot3f(x, x, y, y, z, z);
   };
   const float ab0 = B[0] - A[0], ab1 = B[1] - A[1], ab2 = B[2] - A[2];
   const float ac0 = C[0] - A[0], ac1 = C[1] - A[1], ac2 = C[2] - A[2];
   const float ap0 = P[0] - A[0], ap1 = P[1] - A[1], ap2 = P[2] - A[2];
-  const float d1 = ab0 * ap0 + ab1 * ap1 + ab2 * ap2;
-  const float d2 = ac0 * ap0 + ac1 * ap1 + ac2 * ap2;
+  const float d1 = dot3f(ab0, ap0, ab1, ap1, ab2, ap2);
+  const float d2 = dot3f(ac0, ap0, ac1, ap1, ac2, ap2);
   if(d1 <= 0.f && d2 <= 0.f) return ret(ap0, ap1, ap2);
   const float bp0 = P[0] - B[0], bp1 = P[1] - B[1], bp2 = P[2] - B[2];
-  const float d3 = ab0 * bp0 + ab1 * bp1 + ab2 * bp2;
-  const float d4 = ac0 * bp0 + ac1 * bp1 + ac2 * bp2;
+  const float d3 = dot3f(ab0, bp0, ab1, bp1, ab2, bp2);
+  const float d4 = dot3f(ac0, bp0, ac1, bp1, ac2, bp2);
   if(d3 >= 0.f && d4 <= d3) return ret(bp0, bp1, bp2);
-  const float vc = d1 * d4 - d3 * d2;
+  const float vc = __fmaf_rn(d1, d4, -(d3 * d2));
   if(vc <= 0.f && d1 >= 0.f && d3 <= 0.f)
   {
     const float v = d1 / (d1 - d3);
-    return ret(ap0 - v * ab0, ap1 - v * ab1, ap2 - v * ab2);
+    return ret(__fmaf_rn(-v, ab0, ap0), __fmaf_rn(-v, ab1, ap1), __fmaf_rn(-v, ab2, ap2));
   }
   const float cp0 = P[0] - C[0], cp1 = P[1] - C[1], cp2 = P[2] - C[2];
-  const float d5 = ab0 * cp0 + ab1 * cp1 + ab2 * cp2;
-  const float d6 = ac0 * cp0 + ac1 * cp1 + ac2 * cp2;
+  const float d5 = dot3f(ab0, cp0, ab1, cp1, ab2, cp2);
+  const float d6 = dot3f(ac0, cp0, ac1, cp1, ac2, cp2);
   if(d6 >= 0.f && d5 <= d6) return ret(cp0, cp1, cp2);
-  const float vb = d5 * d2 - d1 * d6;
+  const float vb = __fmaf_rn(d5, d2, -(d1 * d6));
   if(vb <= 0.f && d2 >= 0.f && d6 <= 0.f)
   {
     const float w = d2 / (d2 - d6);
-    return ret(ap0 - w * ac0, ap1 - w * ac1, ap2 - w * ac2);
+    return ret(__fmaf_rn(-w, ac0, ap0), __fmaf_rn(-w, ac1, ap1), __fmaf_rn(-w, ac2, ap2));
   }
-  const float va = d3 * d6 - d5 * d4;
+  const float va = __fmaf_rn(d3, d6, -(d5 * d4));
   if(va <= 0.f && (d4 - d3) >= 0.f && (d5 - d6) >= 0.f)
   {
     const float w = (d4 - d3) / ((d4 - d3) + (d5 - d6));
@@ -85,7 +93,54 @@ __device__ __forceinline__ float dist2_f32(const float* P, const float* A, const
   }
   const float denom = 1.f / (va + vb + vc);
   const float v = vb * denom, w = vc * denom;
-  return ret(ap0 - v * ab0 - w * ac0, ap1 - v * ab1 - w * ac1, ap2 - v * ab2 - w * ac2);
+  return ret(__fmaf_rn(-w, ac0, __fmaf_rn(-v, ab0, ap0)), __fmaf_rn(-w, ac1, __fmaf_rn(-v, ab1, ap1)),
+             __fmaf_rn(-w, ac2, __fmaf_rn(-v, ab2, ap2)));
+}
+
+// dist2_f32 without branches: the same region tests in the same order and the
+// same formulas per region, selected instead of branched to, so that the
+// lanes of a warp testing different triangles do not diverge.  One division
+// serves every region (its operands are selected); the offset is
+// base - v e1 - w e2 with fused operations.
+__device__ __forceinline__ float dist2_f32_flat(const float* P, const float* A, const float* B, const float* C,
+                                               float* off)
+{
+  const float ab0 = B[0] - A[0], ab1 = B[1] - A[1], ab2 = B[2] - A[2];
+  const float ac0 = C[0] - A[0], ac1 = C[1] - A[1], ac2 = C[2] - A[2];
+  const float bc0 = C[0] - B[0], bc1 = C[1] - B[1], bc2 = C[2] - B[2];
+  const float ap0 = P[0] - A[0], ap1 = P[1] - A[1], ap2 = P[2] - A[2];
+  const float bp0 = P[0] - B[0], bp1 = P[1] - B[1], bp2 = P[2] - B[2];
+  const float cp0 = P[0] - C[0], cp1 = P[1] - C[1], cp2 = P[2] - C[2];
+  const float d1 = dot3f(ab0, ap0, ab1, ap1, ab2, ap2);
+  const float d2 = dot3f(ac0, ap0, ac1, ap1, ac2, ap2);
+  const float d3 = dot3f(ab0, bp0, ab1, bp1, ab2, bp2);
+  const float d4 = dot3f(ac0, bp0, ac1, bp1, ac2, bp2);
+  const float d5 = dot3f(ab0, cp0, ab1, cp1, ab2, cp2);
+  const float d6 = dot3f(ac0, cp0, ac1, cp1, ac2, cp2);
+  const float vc = __fmaf_rn(d1, d4, -(d3 * d2));
+  const float vb = __fmaf_rn(d5, d2, -(d1 * d6));
+  const float va = __fmaf_rn(d3, d6, -(d5 * d4));
+  const bool rA = d1 <= 0.f && d2 <= 0.f;
+  const bool rB = !rA && d3 >= 0.f && d4 <= d3;
+  const bool rAB = !rA && !rB && vc <= 0.f && d1 >= 0.f && d3 <= 0.f;
+  const bool rC = !rA && !rB && !rAB && d6 >= 0.f && d5 <= d6;
+  const bool rAC = !rA && !rB && !rAB && !rC && vb <= 0.f && d2 >= 0.f && d6 <= 0.f;
+  const bool rBC = !rA && !rB && !rAB && !rC && !rAC && va <= 0.f && (d4 - d3) >= 0.f && (d5 - d6) >= 0.f;
+  const bool rF = !rA && !rB && !rAB && !rC && !rAC && !rBC;
+  const float num = rAB ? d1 : rAC ? d2 : rBC ? (d4 - d3) : 1.f;
+  const float den = rAB ? (d1 - d3) : rAC ? (d2 - d6) : rBC ? ((d4 - d3) + (d5 - d6)) : rF ? (va + vb + vc) : 1.f;
+  const float t = num / den;
+  const float v = rAB ? t : rF ? vb * t : 0.f;
+  const float w = (rAC || rBC) ? t : rF ? vc * t : 0.f;
+  // base and directions per region: A, AB, AC, face from A; B, BC from B; C from C
+  const bool fromB = rB || rBC, fromC = rC;
+  const float b0 = fromB ? bp0 : fromC ? cp0 : ap0, b1 = fromB ? bp1 : fromC ? cp1 : ap1,
+              b2 = fromB ? bp2 : fromC ? cp2 : ap2;
+  const float e0 = rBC ? bc0 : ac0, e1 = rBC ? bc1 : ac1, e2 = rBC ? bc2 : ac2;
+  off[0] = __fmaf_rn(-w, e0, __fmaf_rn(-v, ab0, b0));
+  off[1] = __fmaf_rn(-w, e1, __fmaf_rn(-v, ab1, b1));
+  off[2] = __fmaf_rn(-w, e2, __fmaf_rn(-v, ab2, b2));
+  return dot3f(off[0], off[0], off[1], off[1], off[2], off[2]);
 }
 
 // Per-query constants of the FP32 certificates.
@@ -151,8 +206,8 @@ __device__ __forceinline__ int box_decide(const float* lo, const float* hi, floa
   const float n0 = (s0 * 0.999f < lim) ? 0.f : 1.f;
   const float n1 = (s1 * 0.999f < lim) ? 0.f : 1.f;
   const float n2 = (s2 * 0.999f < lim) ? 0.f : 1.f;
-  const float d2 = g0 * g0 + g1 * g1 + g2 * g2;
-  const float err = 2.02f * del * (g0 + g1 + g2) + 1.01f * del * del * (n0 + n1 + n2) + 0x1p-21f * d2;
+  const float d2 = dot3f(g0, g0, g1, g1, g2, g2);
+  const float err = __fmaf_rn(0x1p-21f, d2, __fmaf_rn(1.01f * del * del, n0 + n1 + n2, 2.02f * del * (g0 + g1 + g2)));
   if(!(err < INFINITY)) return 2;
   if(__fsub_rd(d2, err) > c.t_false) return 0;
   if(__fadd_ru(d2, err) <= c.t_true) return 1;
@@ -188,7 +243,7 @@ __device__ __forceinline__ bool visit32(const NodeRec32* __restrict__ nodes32, i
       const float sL = lo_l[d] + hi_l[d], sR = lo_r[d] + hi_r[d];
       const float av = sL - sR;
       const float bv = (sL + sR) - 4.f * c.qf[d];
-      dot += av * bv;
+      dot = __fmaf_rn(av, bv, dot);
       mag += fabsf(av) + fabsf(bv);
       prod += fabsf(av * bv);
     }
@@ -260,11 +315,12 @@ __device__ __forceinline__ int leaf_prefilter_bounds(const LeafRec32<NPC>* __res
   const float4* r = reinterpret_cast<const float4*>(leaves32 + leafpos);
   float v[3 * NPC];
   float ec[2], lt[2];
+  float fzt = 0.f;
   if constexpr(NPC == 3)
   {
     const float4 a = __ldg(r), b = __ldg(r + 1), cc = __ldg(r + 2);
     v[0] = a.x, v[1] = a.y, v[2] = a.z, v[3] = a.w, v[4] = b.x, v[5] = b.y, v[6] = b.z, v[7] = b.w, v[8] = cc.x;
-    ec[0] = cc.y, lt[0] = cc.z;
+    ec[0] = cc.y, lt[0] = cc.z, fzt = cc.w;
   }
   else
   {
@@ -284,18 +340,28 @@ __device__ __forceinline__ int leaf_prefilter_bounds(const LeafRec32<NPC>* __res
     const float* B = v + 3 * (s + 1);
     const float* C = v + 3 * (s + 2);
     float off[3];
-    const float d2 = dist2_f32(c.qf, A, B, C, off);
+    const float d2 = dist2_f32_flat(c.qf, A, B, C, off);
     const float ap = fmaxf(fabsf(c.qf[0] - A[0]), fmaxf(fabsf(c.qf[1] - A[1]), fabsf(c.qf[2] - A[2])));
     const float E = __fadd_ru(c.lip, __fmul_ru(ec[s], __fadd_ru(ap, lt[s])));
     const float lim = __fadd_ru(c.thr_leaf, E);
     if(!(d2 > __fmul_ru(__fmul_ru(lim, lim), 1.0f + 0x1p-20f)))
     {
       need |= 1 << s;
-      const float kappa = ec[s] * (1.f / (256.f * 0x1p-24f));
-      const float kl = __fdiv_ru(kappa, lt[s]);
-      const float fz = __fmul_ru(2e-12f, __fadd_ru(kl, __fdiv_ru(__fmul_ru(kl, kl), lt[s])));
-      const float dl = fmaxf(__fsub_rd(__fsqrt_rd(__fmul_rd(d2, 1.f - 0x1p-20f)), E), 0.f);
-      const float dh = __fadd_ru(__fadd_ru(__fsqrt_ru(__fmul_ru(d2, 1.f + 0x1p-20f)), E), fz);
+      float fz;
+      if constexpr(NPC == 3)
+        fz = fzt;  // stored with the triangle
+      else
+      {
+        const float kappa = ec[s] * (1.f / (256.f * 0x1p-24f));
+        const float kl = __fdiv_ru(kappa, lt[s]);
+        fz = __fmul_ru(2e-12f, __fadd_ru(kl, __fdiv_ru(__fmul_ru(kl, kl), lt[s])));
+      }
+      // sqrt(d2 (1 -+ 2^-20)) from the correctly rounded sqrt(d2): the factor
+      // 1 -+ 2^-20 covers both the 2^-21 of the square root of the margin and
+      // the 2^-24 rounding of sqrtf
+      const float sd = sqrtf(d2);
+      const float dl = fmaxf(__fsub_rd(__fmul_rd(sd, 1.f - 0x1p-20f), E), 0.f);
+      const float dh = __fadd_ru(__fadd_ru(__fmul_ru(sd, 1.f + 0x1p-20f), E), fz);
       const float l2 = __fmul_rd(dl, dl), h2 = __fmul_ru(dh, dh);
       lo2 = (d2 == d2) ? fminf(lo2, l2) : 0.f;
       hi2 = (d2 == d2 && h2 == h2) ? fminf(hi2, h2) : hi2;
