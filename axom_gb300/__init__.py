@@ -10,6 +10,11 @@ the reference:
 * ``SignedDistance`` -- ``quest::SignedDistance<3, Exec>``
   (quest/SignedDistance.hpp:147-605): ``compute_distance``,
   ``compute_distances``, ``get_mesh_bounds``, ``get_bvh_tree``.
+* ``ClosestPoint``   -- the local query of ``quest::DistributedClosestPoint``
+  (quest/detail/DistributedClosestPointImpl.hpp:883-901, 1002-1050):
+  ``set_distance_threshold``, ``compute_closest_points``.
+* ``Batch``          -- many meshes and point sets in one CUDA graph (no
+  reference counterpart).
 
 Arrays may be numpy arrays (host memory) or torch tensors (host or CUDA); the
 C ABI classifies each pointer.  Outputs are numpy arrays for host inputs and
@@ -23,7 +28,8 @@ from pathlib import Path
 
 import numpy as np
 
-__all__ = ["GsqError", "BVH", "SignedDistance", "Batch", "load", "PRECISION_FP64", "PRECISION_MIXED"]
+__all__ = ["GsqError", "BVH", "SignedDistance", "ClosestPoint", "Batch", "load", "PRECISION_FP64",
+           "PRECISION_MIXED"]
 
 PKG = Path(__file__).resolve().parent
 LIB_PATH = PKG / "libgsq.so"
@@ -94,6 +100,10 @@ SIGNATURES = [
     ("gsq_sdf_mixed_stats", C.c_int, [_vp, _i64p]),
     ("gsq_sdf_backward", C.c_int, [_vp, _vp, _vp, _vp, C.c_int32, C.c_int32, _vp, _vp, _vp, _vp]),
     ("gsq_sdf_eval_noalloc", C.c_int, [_vp, _vp, _vp, _vp, C.c_int32, C.c_int32, _vp, _vp]),
+    ("gsq_cpq_create", C.c_int, [C.POINTER(_vp), _vp, C.c_int32, _vp, _vp]),
+    ("gsq_cpq_destroy", C.c_int, [_vp]),
+    ("gsq_cpq_query", C.c_int, [_vp, _vp, C.c_int32, C.c_double, C.c_int32, _vp, _vp, _vp, _vp, _vp]),
+    ("gsq_cpq_last_ms", C.c_int, [_vp, C.POINTER(C.c_float)]),
     ("gsq_batch_opts_init", C.c_int, [_vp]),
     ("gsq_batch_create", C.c_int, [C.POINTER(_vp), C.c_int32, _vp, _vp, _vp, C.c_int32, _vp, C.c_int32, C.c_int32,
                                    _vp, _vp]),
@@ -515,4 +525,46 @@ class Batch:
     def max_depth(self) -> int:
         v = C.c_int32()
         _check(self._lib.gsq_batch_max_depth(self._h, C.byref(v)))
+        return v.value
+
+
+class ClosestPoint:
+    """The local closest-point query of quest::DistributedClosestPoint
+    (quest/detail/DistributedClosestPointImpl.hpp:883-901, 1002-1050): a BVH
+    over ``points`` (n, 3) with optional per-point ``domain_ids``, then for each
+    query point the closest object point within ``distance_threshold``."""
+
+    def __init__(self, points, domain_ids=None):
+        self._lib = load()
+        p = _Arr(points, np.float64, 3)
+        d = _Arr(domain_ids, np.int32) if domain_ids is not None else None
+        h = _vp()
+        _check(self._lib.gsq_cpq_create(C.byref(h), C.c_void_p(p.ptr), p.n, C.c_void_p(d.ptr) if d else None,
+                                        _stream()))
+        self._h = h
+        self.sq_threshold = float(np.finfo(np.float64).max)
+
+    def __del__(self):
+        if getattr(self, "_h", None):
+            self._lib.gsq_cpq_destroy(self._h)
+            self._h = None
+
+    def set_distance_threshold(self, t: float):
+        """DistributedClosestPoint::setDistanceThreshold: stores t * t."""
+        self.sq_threshold = float(t) * float(t)
+
+    def compute_closest_points(self, queries, precision: int = PRECISION_MIXED):
+        """(index (m,), domain (m,), position (m, 3), distance (m,)); -1 / NaN where none."""
+        q = _Arr(queries, np.float64, 3)
+        m = q.n
+        idx, dom = q.empty(m, np.int32), q.empty(m, np.int32)
+        pos, dist = q.empty((m, 3), np.float64), q.empty(m, np.float64)
+        _check(self._lib.gsq_cpq_query(self._h, C.c_void_p(q.ptr), m, self.sq_threshold, precision,
+                                       C.c_void_p(_ptr(idx)), C.c_void_p(_ptr(dom)), C.c_void_p(_ptr(pos)),
+                                       C.c_void_p(_ptr(dist)), _stream()))
+        return idx, dom, pos, dist
+
+    def last_query_ms(self) -> float:
+        v = C.c_float()
+        _check(self._lib.gsq_cpq_last_ms(self._h, C.byref(v)))
         return v.value

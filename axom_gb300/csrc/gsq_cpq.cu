@@ -1,0 +1,345 @@
+// Closest object point: the local query of quest::DistributedClosestPoint on
+// the GPU.
+//
+// Reference: quest/detail/DistributedClosestPointImpl.hpp.  The object points
+// become one degenerate box each in a spin::BVH with the default scale
+// factor (generateBVHTreeImpl, 883-901); computeLocalClosestPoints (1002-1050)
+// then runs, per query point, the point traverser (nearer centroid first,
+// spin/policy/LinearBVH.hpp:72-85) with the predicate
+//   squared_distance(p, box) <= best && squared_distance(p, box) <= threshold
+// and the leaf action "replace the best if strictly closer" (the first point
+// found wins ties).  Not found: index and domain -1, position and distance NaN.
+//
+// Two forms, equal bit for bit: FP64 (every decision in FP64, the reference's
+// operation order), and mixed (node decisions certified in FP32 on outward
+// rounded boxes, undecided ones and every point distance in FP64).
+#include "gsq_sdf_handle.cuh"
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <new>
+
+namespace gsq
+{
+gsq_bvh* bvh_new_internal(int device);
+int bvh_build_internal(gsq_bvh* h, const double* d_boxes, int n, cudaStream_t s);
+
+namespace
+{
+using namespace sdf;
+
+// One sorted leaf: the object point, its index and its domain id.
+struct __align__(16) PointRec
+{
+  double p[3];
+  int id;
+  int dom;
+};
+static_assert(sizeof(PointRec) == 32, "point record is 32 bytes");
+
+__global__ void k_point_boxes(const double* __restrict__ pts, int n, double* __restrict__ boxes)
+{
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if(i >= n) return;
+  for(int d = 0; d < 3; ++d)
+  {
+    const double v = pts[3 * (size_t)i + d];
+    boxes[6 * (size_t)i + d] = v;
+    boxes[6 * (size_t)i + 3 + d] = v;
+  }
+}
+
+__global__ void k_point_records(const int* __restrict__ perm, int nleaves, const double* __restrict__ pts,
+                                const int* __restrict__ dom, int n, PointRec* __restrict__ recs)
+{
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if(k >= nleaves) return;
+  const int c = perm[k];
+  PointRec r;
+  const bool ok = c < n;  // padding leaves of a 0/1-point cloud are never reached
+  for(int d = 0; d < 3; ++d) r.p[d] = ok ? pts[3 * (size_t)c + d] : 0.0;
+  r.id = ok ? c : -1;
+  r.dom = (ok && dom) ? dom[c] : (ok ? 0 : -1);
+  recs[k] = r;
+}
+
+__global__ void k_cpq_codes(const double* __restrict__ q, int m, const double* b, uint32_t* __restrict__ codes)
+{
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if(i >= m) return;
+  uint32_t u[3];
+  for(int d = 0; d < 3; ++d)
+  {
+    const double ext = b[3 + d] - b[d];
+    const double sc = (ext > 0.0) ? 1.0 / ext : 0.0;
+    u[d] = (uint32_t)(int)fmin(fmax((q[3 * (size_t)i + d] - b[d]) * sc * 1024.0, 0.0), 1023.0);
+  }
+  auto spread = [](uint32_t x) {
+    x = (x | (x << 16)) & 0xFF0000FFu;
+    x = (x | (x << 8)) & 0x0F00F00Fu;
+    x = (x | (x << 4)) & 0xC30C30C3u;
+    x = (x | (x << 2)) & 0x49249249u;
+    return x;
+  };
+  codes[i] = spread(u[0]) | (spread(u[1]) << 1) | (spread(u[2]) << 2);
+}
+
+// The point traverser's FP64 node step with the closest-point predicate.
+__device__ __forceinline__ void cpq_visit_fp64(const NodeRec64* __restrict__ nodes, int cur, const double* q,
+                                               double best, double thr, bool& inL, bool& inR, bool& swap)
+{
+  const double2* r = reinterpret_cast<const double2*>(nodes + cur);
+  double b[12];
+#pragma unroll
+  for(int k = 0; k < 6; ++k)
+  {
+    const double2 t = __ldg(r + k);
+    b[2 * k] = t.x;
+    b[2 * k + 1] = t.y;
+  }
+  inL = false;
+  inR = false;
+  if(box_valid(b, b + 3))
+  {
+    const double sq = sqdist_pb(q, b, b + 3);
+    inL = sq <= best && sq <= thr;
+  }
+  if(box_valid(b + 6, b + 9))
+  {
+    const double sq = sqdist_pb(q, b + 6, b + 9);
+    inR = sq <= best && sq <= thr;
+  }
+  swap = false;
+  if(inL && inR)
+  {
+    const double cl[3] = {0.5 * (b[0] + b[3]), 0.5 * (b[1] + b[4]), 0.5 * (b[2] + b[5])};
+    const double cr[3] = {0.5 * (b[6] + b[9]), 0.5 * (b[7] + b[10]), 0.5 * (b[8] + b[11])};
+    swap = sqdist_pp(q, cl) > sqdist_pp(q, cr);
+  }
+}
+
+template <bool MIXED>
+__global__ void __launch_bounds__(128) k_cpq(const NodeRec64* __restrict__ nodes64,
+                                             const NodeRec32* __restrict__ nodes32,
+                                             const PointRec* __restrict__ recs,
+                                             const double* __restrict__ qs,
+                                             int m,
+                                             const int* __restrict__ order,
+                                             double thr,
+                                             float coord_max,
+                                             int* __restrict__ out_idx,
+                                             int* __restrict__ out_dom,
+                                             double* __restrict__ out_pos,
+                                             double* __restrict__ out_dist,
+                                             int* err)
+{
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if(t >= m) return;
+  const int i = order ? __ldg(order + t) : t;
+  const double q[3] = {qs[3 * (size_t)i], qs[3 * (size_t)i + 1], qs[3 * (size_t)i + 2]};
+  double best = DBL_MAX;
+  int bid = -1, bdom = -1, bleaf = -1;
+  QCtx c;
+  if(MIXED)
+  {
+    qctx_init(c, q, coord_max);
+    qctx_update(c, fmin(best, thr));
+  }
+  auto visit = [&](int cur, bool& inL, bool& inR, bool& swap, int2& ch) {
+    if(MIXED && visit32(nodes32, cur, c, inL, inR, swap, ch)) return;
+    ch = __ldg(reinterpret_cast<const int2*>(nodes64[cur].child));
+    cpq_visit_fp64(nodes64, cur, q, best, thr, inL, inR, swap);
+  };
+  auto leaf = [&](int leafpos) {
+    const PointRec r = recs[leafpos];
+    if(r.id < 0) return;
+    const double sq = sqdist_pp(q, r.p);
+    if(sq < best)
+    {
+      best = sq;
+      bid = r.id;
+      bdom = r.dom;
+      bleaf = leafpos;
+      if(MIXED) qctx_update(c, fmin(best, thr));
+    }
+  };
+  if(!traverse_point(visit, leaf)) atomicOr(err, DEVERR_STACK);
+  out_idx[i] = bid;
+  out_dom[i] = bdom;
+  const double nan = __longlong_as_double(0x7ff8000000000000LL);
+  const PointRec* r = (bleaf >= 0) ? recs + bleaf : nullptr;
+  for(int d = 0; d < 3; ++d) out_pos[3 * (size_t)i + d] = r ? r->p[d] : nan;
+  out_dist[i] = r ? sqrt(best) : nan;
+}
+
+inline int grid_for(long long n, int threads) { return (int)std::max<long long>(1, (n + threads - 1) / threads); }
+}  // namespace
+}  // namespace gsq
+
+using namespace gsq;
+
+struct gsq_cpq
+{
+  int device = 0;
+  int n = 0;
+  gsq_bvh* bvh = nullptr;
+  PointRec* recs = nullptr;
+  NodeRec32* nodes32 = nullptr;
+  double* d_bounds = nullptr;
+  float coord_max = 0.f;
+  int* d_err = nullptr;
+  float eval_ms = 0.f;
+};
+
+namespace
+{
+void cpq_release(gsq_cpq* h)
+{
+  if(h->recs) cudaFree(h->recs);
+  if(h->nodes32) cudaFree(h->nodes32);
+  if(h->d_bounds) cudaFree(h->d_bounds);
+  if(h->d_err) cudaFree(h->d_err);
+  if(h->bvh) gsq_bvh_destroy(h->bvh);
+  delete h;
+}
+}  // namespace
+
+extern "C" {
+
+int gsq_cpq_create(gsq_cpq** out, const double* points, int32_t n, const int32_t* domain_ids, void* stream)
+{
+  if(!out) return fail(GSQ_ERR_INVALID, "null output pointer");
+  *out = nullptr;
+  if(n < 0 || n >= (1 << 30)) return fail(GSQ_ERR_INVALID, "number of points must be 0..2^30-1");
+  if(n > 0 && !points) return fail(GSQ_ERR_INVALID, "null point array");
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  auto* h = new(std::nothrow) gsq_cpq();
+  if(!h) return fail(GSQ_ERR_NOMEM, "handle allocation failed");
+  auto bail = [&](int rc) {
+    cpq_release(h);
+    return rc;
+  };
+  h->n = n;
+  cudaError_t e = cudaGetDevice(&h->device);
+  if(e == cudaSuccess) e = cudaMalloc(&h->d_err, sizeof(int));
+  if(e == cudaSuccess) e = cudaMemsetAsync(h->d_err, 0, sizeof(int), s);
+  if(e == cudaSuccess) e = cudaMalloc(&h->d_bounds, 6 * sizeof(double));
+  if(e != cudaSuccess) return bail(cuda_fail(e, "gsq_cpq_create"));
+  InBuf pb, db;
+  e = pb.stage(points, sizeof(double) * 3 * (size_t)n, s);
+  if(e == cudaSuccess) e = db.stage(domain_ids, domain_ids ? sizeof(int) * (size_t)n : 0, s);
+  if(e != cudaSuccess) return bail(cuda_fail(e, "gsq_cpq_create: points"));
+  Scratch boxes;
+  e = boxes.alloc(sizeof(double) * 6 * (size_t)std::max(n, 1), s);
+  if(e != cudaSuccess) return bail(cuda_fail(e, "gsq_cpq_create: boxes"));
+  if(n > 0)
+  {
+    k_point_boxes<<<grid_for(n, 256), 256, 0, s>>>(static_cast<const double*>(pb.dev), n, boxes.as<double>());
+    count_launch();
+  }
+  h->bvh = bvh_new_internal(h->device);
+  if(!h->bvh) return bail(GSQ_ERR_NOMEM);
+  int rc = bvh_build_internal(h->bvh, boxes.as<double>(), n, s);
+  if(rc) return bail(rc);
+  const BvhDev* B = bvh_dev(h->bvh);
+  e = cudaMalloc(&h->recs, sizeof(PointRec) * B->n);
+  if(e == cudaSuccess) e = cudaMalloc(&h->nodes32, sizeof(NodeRec32) * std::max(B->n - 1, 1));
+  if(e != cudaSuccess) return bail(cuda_fail(e, "gsq_cpq_create: records"));
+  k_point_records<<<grid_for(B->n, 256), 256, 0, s>>>(B->perm, B->n, static_cast<const double*>(pb.dev),
+                                                      static_cast<const int*>(db.dev), n, h->recs);
+  count_launch();
+  rc = mixed_prepare(B->nodes, B->n - 1, nullptr, 0, 3, h->nodes32, nullptr, s);
+  if(rc) return bail(rc);
+  double mm = 0.0;
+  for(int d = 0; d < 6; ++d)
+    if(std::fabs(B->bounds[d]) < DBL_MAX) mm = std::max(mm, std::fabs(B->bounds[d]));
+  h->coord_max = (float)(mm * (1.0 + 1e-6));
+  e = cudaMemcpyAsync(h->d_bounds, B->bounds, 6 * sizeof(double), cudaMemcpyHostToDevice, s);
+  if(e == cudaSuccess) e = cudaStreamSynchronize(s);
+  if(e != cudaSuccess) return bail(cuda_fail(e, "gsq_cpq_create"));
+  rc = check_device_error(h->d_err, s, "gsq_cpq_create");
+  if(rc) return bail(rc);
+  *out = h;
+  return GSQ_OK;
+}
+
+int gsq_cpq_destroy(gsq_cpq* h)
+{
+  if(h) cpq_release(h);
+  return GSQ_OK;
+}
+
+int gsq_cpq_query(const gsq_cpq* hc, const double* points, int32_t m, double sq_threshold, int32_t precision,
+                  int32_t* idx, int32_t* dom, double* pos, double* dist, void* stream)
+{
+  gsq_cpq* h = const_cast<gsq_cpq*>(hc);
+  if(!h) return fail(GSQ_ERR_INVALID, "null closest-point handle");
+  if(m < 0) return fail(GSQ_ERR_INVALID, "negative point count");
+  if(m == 0) return GSQ_OK;
+  if(!points || !idx || !dom || !pos || !dist) return fail(GSQ_ERR_INVALID, "null point or output array");
+  if(precision != GSQ_PRECISION_FP64 && precision != GSQ_PRECISION_MIXED)
+    return fail(GSQ_ERR_INVALID, "unknown precision");
+  if(!(sq_threshold >= 0.0)) return fail(GSQ_ERR_INVALID, "the squared threshold must be >= 0");
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  InBuf qb;
+  GSQ_CUDA_TRY(qb.stage(points, sizeof(double) * 3 * (size_t)m, s));
+  OutBuf ib, dmb, pb, sb;
+  GSQ_CUDA_TRY(ib.prepare(idx, sizeof(int) * (size_t)m, s));
+  GSQ_CUDA_TRY(dmb.prepare(dom, sizeof(int) * (size_t)m, s));
+  GSQ_CUDA_TRY(pb.prepare(pos, sizeof(double) * 3 * (size_t)m, s));
+  GSQ_CUDA_TRY(sb.prepare(dist, sizeof(double) * (size_t)m, s));
+  const double* q = static_cast<const double*>(qb.dev);
+
+  // Morton order of the query points (processing order only)
+  Scratch ob;
+  const int* order = nullptr;
+  if(m > 1)
+  {
+    GSQ_CUDA_TRY(ob.alloc(4 * sizeof(uint32_t) * (size_t)m, s));
+    uint32_t* keys[2] = {ob.as<uint32_t>(), ob.as<uint32_t>() + m};
+    int* vals[2] = {reinterpret_cast<int*>(ob.as<uint32_t>() + 2 * (size_t)m),
+                    reinterpret_cast<int*>(ob.as<uint32_t>() + 3 * (size_t)m)};
+    k_cpq_codes<<<grid_for(m, 256), 256, 0, s>>>(q, m, h->d_bounds, keys[0]);
+    count_launch();
+    const int which = radix_sort_pairs(keys, vals, m, 30, true, s, h->d_err);
+    if(which < 0) return which;
+    order = vals[which];
+  }
+  const BvhDev* B = bvh_dev(h->bvh);
+  cudaEvent_t e0, e1;
+  GSQ_CUDA_TRY(cudaEventCreate(&e0));
+  GSQ_CUDA_TRY(cudaEventCreate(&e1));
+  cudaEventRecord(e0, s);
+  if(precision == GSQ_PRECISION_MIXED)
+    k_cpq<true><<<grid_for(m, 128), 128, 0, s>>>(B->nodes, h->nodes32, h->recs, q, m, order, sq_threshold,
+                                                 h->coord_max, static_cast<int*>(ib.dev), static_cast<int*>(dmb.dev),
+                                                 static_cast<double*>(pb.dev), static_cast<double*>(sb.dev), h->d_err);
+  else
+    k_cpq<false><<<grid_for(m, 128), 128, 0, s>>>(B->nodes, h->nodes32, h->recs, q, m, order, sq_threshold,
+                                                  h->coord_max, static_cast<int*>(ib.dev),
+                                                  static_cast<int*>(dmb.dev), static_cast<double*>(pb.dev),
+                                                  static_cast<double*>(sb.dev), h->d_err);
+  count_launch();
+  cudaEventRecord(e1, s);
+  cudaError_t e = cudaGetLastError();
+  if(e == cudaSuccess) e = ib.flush(s);
+  if(e == cudaSuccess) e = dmb.flush(s);
+  if(e == cudaSuccess) e = pb.flush(s);
+  if(e == cudaSuccess) e = sb.flush(s);
+  if(e == cudaSuccess) e = cudaStreamSynchronize(s);
+  if(e == cudaSuccess) e = cudaEventElapsedTime(&h->eval_ms, e0, e1);
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  if(e != cudaSuccess) return cuda_fail(e, "gsq_cpq_query");
+  return check_device_error(h->d_err, s, "gsq_cpq_query");
+}
+
+int gsq_cpq_last_ms(const gsq_cpq* h, float* ms)
+{
+  if(!h || !ms) return fail(GSQ_ERR_INVALID, "null argument");
+  *ms = h->eval_ms;
+  return GSQ_OK;
+}
+
+}  // extern "C"

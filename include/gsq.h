@@ -233,6 +233,29 @@ int gsq_sdf_backward(const gsq_sdf* sdf, const double* qx, const double* qy, con
  * No reference counterpart (the reference has only the FP64 form). */
 int gsq_sdf_mixed_stats(const gsq_sdf* sdf, int64_t* counters);
 
+/* ---- Closest object point ----------------------------------------------
+ * Replaces the local step of quest::DistributedClosestPoint
+ * (quest/detail/DistributedClosestPointImpl.hpp: generateBVHTreeImpl 883-901,
+ * computeLocalClosestPoints 1002-1050): a BVH over the object points (one
+ * degenerate box each, default scale factor), then per query point the closest
+ * object point within a distance threshold.  MPI exchange and conduit
+ * plumbing are not part of it (one GPU, one domain set).
+ *   points      n x 3 object points (host or device); domain_ids n ints (nullable = 0)
+ *   sq_threshold  squared distance threshold (the reference's
+ *               setDistanceThreshold(t) stores t*t; DBL_MAX = none)
+ *   idx, dom    m ints: the closest object point and its domain, -1 if none
+ *   pos, dist   m x 3 and m doubles: its coordinates and distance, NaN if none
+ *   precision   GSQ_PRECISION_FP64 or GSQ_PRECISION_MIXED (FP32-certified node
+ *               decisions); both give the same bits.
+ * Ties keep the first point the traversal reaches, as the reference does. */
+typedef struct gsq_cpq gsq_cpq;
+int gsq_cpq_create(gsq_cpq** out, const double* points, int32_t n, const int32_t* domain_ids, void* stream);
+int gsq_cpq_destroy(gsq_cpq* cpq);
+int gsq_cpq_query(const gsq_cpq* cpq, const double* points, int32_t m, double sq_threshold, int32_t precision,
+                  int32_t* idx, int32_t* dom, double* pos, double* dist, void* stream);
+/* Milliseconds of device time of the last query kernel. */
+int gsq_cpq_last_ms(const gsq_cpq* cpq, float* ms);
+
 /* ---- Batched signed distance -------------------------------------------
  * Many independent surface meshes, each with its own set of query points of
  * any size, evaluated together.  One run rebuilds the BVH of every mesh (a

@@ -123,6 +123,26 @@ class _Lib:
         p = _arr(p, np.float64).reshape(-1, 3)
         return self._csr(self.f("bvh_find_points"), h, p, p.shape[0], _p(p), p.shape[0])
 
+    # ---- closest object point (DistributedClosestPoint's local query) -----
+    def cp(self, pts, domains=None):
+        p = _arr(pts, np.float64).reshape(-1, 3)
+        d = _arr(domains, np.int32) if domains is not None else None
+        fn = self.f("cp_create")
+        fn.restype, fn.argtypes = C.c_void_p, [_dp, C.c_int, _ip]
+        self.f("cp_destroy").argtypes = [C.c_void_p]
+        return _Handle(self, fn(_p(p), p.shape[0], _p(d)), "cp_destroy")
+
+    def cp_query(self, h, q, sq_threshold=float(np.finfo(np.float64).max), threads=1):
+        """(index, domain, position (m,3), distance) per query point."""
+        q = _arr(q, np.float64).reshape(-1, 3)
+        m = q.shape[0]
+        idx, dom = np.empty(m, np.int32), np.empty(m, np.int32)
+        pos, dist = np.empty((m, 3)), np.empty(m)
+        fn = self.f("cp_query")
+        fn.argtypes = [C.c_void_p, _dp, C.c_int, C.c_double, _ip, _ip, _dp, _dp, C.c_int]
+        fn(h.ptr, _p(q), m, sq_threshold, _p(idx), _p(dom), _p(pos), _p(dist), threads)
+        return idx, dom, pos, dist
+
     def internals(self, boxes, scale=1.000123):
         boxes = _arr(boxes, np.float64).reshape(-1, 6)
         n = boxes.shape[0]

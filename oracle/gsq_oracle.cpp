@@ -17,6 +17,7 @@
 #include <cstdint>
 #include <cstdlib>
 #include <cstring>
+#include <limits>
 #include <numeric>
 #include <vector>
 #ifdef _OPENMP
@@ -907,6 +908,85 @@ void orc_sdf_counts(void* h, const double* q, int m, int* box_tests, int* leaf_t
   {
     double d;
     sdf_point(M, q + 3 * (long long)i, &d, nullptr, nullptr, box_tests + i, leaf_tests + i);
+  }
+}
+
+// ---- closest object point (DistributedClosestPoint's local query) ----------
+// The object points, one degenerate box each (BoxType{point},
+// quest/detail/DistributedClosestPointImpl.hpp:883-901), in a BVH with the
+// default scale factor.
+struct PointCloud
+{
+  Tree tree;
+  std::vector<double> xyz;
+  std::vector<int> dom;
+};
+
+void* orc_cp_create(const double* pts, int n, const int* domains)
+{
+  auto* P = new PointCloud();
+  P->xyz.assign(pts, pts + 3 * (long long)std::max(n, 0));
+  P->dom.resize(std::max(n, 0));
+  for(int i = 0; i < n; ++i) P->dom[i] = domains ? domains[i] : 0;
+  std::vector<Box> boxes(std::max(n, 0));
+  for(int i = 0; i < n; ++i)
+    for(int d = 0; d < 3; ++d) boxes[i].lo[d] = boxes[i].hi[d] = pts[3 * (long long)i + d];
+  initialize(P->tree, boxes.data(), n, 1.000123);  // BVH.hpp:410
+  return P;
+}
+
+void orc_cp_destroy(void* h) { delete static_cast<PointCloud*>(h); }
+
+// computeLocalClosestPoints per query point with no earlier candidate
+// (DistributedClosestPointImpl.hpp:1002-1050): the point traverser (nearer
+// centroid first, LinearBVH.hpp:72-85), a branch is entered when its box is
+// within both the best squared distance so far and the threshold, and a point
+// replaces the best only if strictly closer.  Not found: index and domain -1,
+// position and distance NaN.
+void orc_cp_query(void* h, const double* q, int m, double sq_threshold, int* idx, int* dom, double* pos, double* dist,
+                  int nthreads)
+{
+  const PointCloud& P = *static_cast<PointCloud*>(h);
+  if(nthreads < 1) nthreads = 1;
+  const double nan = std::numeric_limits<double>::quiet_NaN();
+#pragma omp parallel for num_threads(nthreads) schedule(dynamic, 64)
+  for(int i = 0; i < m; ++i)
+  {
+    const double* p = q + 3 * (long long)i;
+    double best = DBL_MAX;
+    int bi = -1, bd = -1;
+    auto pred = [&](const Box& bb) {
+      const double sq = sq_dist_pb(p, bb);
+      return sq <= best && sq <= sq_threshold;
+    };
+    auto leaf = [&](int leafpos) {
+      const int c = P.tree.perm[leafpos];
+      if(c >= (int)P.dom.size()) return;  // padding of a 0/1-point cloud
+      const double sq = sq_dist_pp(p, &P.xyz[3 * (long long)c]);
+      if(sq < best)
+      {
+        best = sq;
+        bi = c;
+        bd = P.dom[c];
+      }
+    };
+    auto pref = [&](const Box& l, const Box& r) {
+      double cl[3], cr[3];
+      for(int d = 0; d < 3; ++d) cl[d] = 0.5 * (l.lo[d] + l.hi[d]);
+      const double sl = sq_dist_pp(p, cl);
+      double sr = DBL_MAX;
+      if(valid(r))
+      {
+        for(int d = 0; d < 3; ++d) cr[d] = 0.5 * (r.lo[d] + r.hi[d]);
+        sr = sq_dist_pp(p, cr);
+      }
+      return sl > sr;
+    };
+    traverse(P.tree, pred, leaf, pref);
+    idx[i] = bi;
+    dom[i] = bd;
+    for(int d = 0; d < 3; ++d) pos[3 * (long long)i + d] = (bi >= 0) ? P.xyz[3 * (long long)bi + d] : nan;
+    dist[i] = (bi >= 0) ? std::sqrt(best) : nan;
   }
 }
 

@@ -24,6 +24,7 @@
 #include <cstdint>
 #include <cstdlib>
 #include <cstring>
+#include <limits>
 #include <vector>
 #ifdef _OPENMP
 #include <omp.h>
@@ -310,6 +311,74 @@ void ref_sdf_mesh_bounds(void* hv, double* out6)
   BoxType bb;
   for(size_t i = 0; i < h->x.size(); ++i) bb.addPoint(PointType {h->x[i], h->y[i], h->z[i]});
   put_box(bb, out6);
+}
+
+// ---- the local closest-point query of quest::DistributedClosestPoint --------
+// DistributedClosestPoint itself needs MPI and conduit; its local step
+// (computeLocalClosestPoints, quest/detail/DistributedClosestPointImpl.hpp:
+// 883-901 and 1002-1050) is a BVH over one degenerate box per object point
+// and a traverse_tree call per query point.  This drives the reference's own
+// BVH and traverser with a leaf action and predicate that behave as that
+// step's (no earlier rank's candidate).
+struct CPHandle
+{
+  BVHType bvh;
+  std::vector<PointType> pts;
+  std::vector<int> dom;
+};
+
+void* ref_cp_create(const double* p, int n, const int* domains)
+{
+  ensure_logger();
+  auto* h = new CPHandle();
+  h->pts.resize(n);
+  h->dom.resize(n);
+  std::vector<BoxType> boxes(n);
+  for(int i = 0; i < n; ++i)
+  {
+    h->pts[i] = PointType {p[3 * i], p[3 * i + 1], p[3 * i + 2]};
+    h->dom[i] = domains ? domains[i] : 0;
+    boxes[i] = BoxType {h->pts[i]};
+  }
+  h->bvh.initialize(boxes.data(), n);
+  return h;
+}
+
+void ref_cp_destroy(void* h) { delete static_cast<CPHandle*>(h); }
+
+void ref_cp_query(void* hv, const double* q, int m, double sq_threshold, int* idx, int* dom, double* pos, double* dist,
+                  int nthreads)
+{
+  auto* h = static_cast<CPHandle*>(hv);
+  auto it = h->bvh.getTraverser();
+  const double nan = std::numeric_limits<double>::quiet_NaN();
+  if(nthreads < 1) nthreads = 1;
+#pragma omp parallel for num_threads(nthreads) schedule(dynamic, 256)
+  for(int i = 0; i < m; ++i)
+  {
+    PointType qpt {q[3 * i], q[3 * i + 1], q[3 * i + 2]};
+    double best = axom::numerics::floating_point_limits<double>::max();
+    int bi = -1, bd = -1;
+    auto leaf = [&](std::int32_t node, const std::int32_t* leaves) {
+      const int c = leaves[node];
+      const double sq = axom::primal::squared_distance(qpt, h->pts[c]);
+      if(sq < best)
+      {
+        best = sq;
+        bi = c;
+        bd = h->dom[c];
+      }
+    };
+    auto pred = [&](const PointType& pt, const BoxType& bb) -> bool {
+      const double sq = axom::primal::squared_distance(pt, bb);
+      return sq <= best && sq <= sq_threshold;
+    };
+    if(!h->pts.empty()) it.traverse_tree(qpt, leaf, pred);
+    idx[i] = bi;
+    dom[i] = bd;
+    for(int d = 0; d < 3; ++d) pos[3 * i + d] = (bi >= 0) ? h->pts[bi][d] : nan;
+    dist[i] = (bi >= 0) ? std::sqrt(best) : nan;
+  }
 }
 
 }  // extern "C"

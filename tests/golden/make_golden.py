@@ -61,10 +61,33 @@ def sdf_fixture(R, name, v, f, q, watertight=True, sign=True):
                         box_tests=nb, leaf_tests=nl, mesh_bounds=R.mesh_bounds(h), watertight=watertight, sign=sign)
 
 
+def cp_fixture(R):
+    """The local closest-point query of DistributedClosestPoint: object points
+    (a sixth of them exact duplicates, so ties occur) with domain ids; query
+    points uniform in the 1.2x box plus some exactly on object points; results
+    without a threshold and with threshold 0.05 (squared 0.0025)."""
+    r = W.rng(21)
+    pts = r.uniform(0.0, 1.0, size=(3000, 3))
+    pts[2500:] = pts[:500]
+    dom = r.integers(0, 5, size=3000).astype(np.int32)
+    q = r.uniform(-0.1, 1.1, size=(3000, 3))
+    q[:300] = pts[1000:1300]
+    h = R.cp(pts, dom)
+    out = {"points": pts, "domains": dom, "queries": q}
+    for tag, thr in (("all", float(np.finfo(np.float64).max)), ("thr", 0.05 * 0.05)):
+        idx, d, pos, dist = R.cp_query(h, q, thr)
+        out.update({f"{tag}_idx": idx, f"{tag}_dom": d, f"{tag}_pos": pos, f"{tag}_dist": dist})
+    np.savez_compressed(OUT / "cp_points3000.npz", **out)
+
+
 def main():
     if oracle.build_reference() is None:
         raise SystemExit("reference sources not found; fixtures can only be made where they are mounted")
     R = oracle.Ref()
+    if sys.argv[1:] == ["cp"]:  # only the closest-point fixture
+        cp_fixture(R)
+        return
+    cp_fixture(R)
     bvh_fixture(R)
     # UV sphere of quest_signed_distance.cpp:86-169 on its 16^3 grid over the
     # sphere box expanded by 2.0

@@ -175,6 +175,38 @@ def test_port_matches_reference_sdf_live(port, ref):
         assert_bits_equal(a[2], b[2], "normals")
 
 
+@pytest.mark.parametrize("tag", ["all", "thr"])
+def test_port_closest_point_matches_golden(port, tag):
+    """DistributedClosestPoint's local query against the reference's outputs."""
+    g = golden("cp_points3000")
+    thr = float(np.finfo(np.float64).max) if tag == "all" else 0.05 * 0.05
+    h = port.cp(g["points"], g["domains"])
+    idx, dom, pos, dist = port.cp_query(h, g["queries"], thr, threads=4)
+    assert_bits_equal(idx, g[f"{tag}_idx"], "index")
+    assert_bits_equal(dom, g[f"{tag}_dom"], "domain")
+    assert_bits_equal(pos, g[f"{tag}_pos"], "position")
+    assert_bits_equal(dist, g[f"{tag}_dist"], "distance")
+
+
+@pytest.mark.parametrize("n", [0, 1, 2, 5000])
+def test_port_closest_point_matches_reference_live(port, ref, n):
+    """Empty and one-point clouds (padded trees), ties from duplicate points,
+    points on the queries, a threshold."""
+    r = np.random.default_rng(30 + n)
+    pts = r.uniform(0, 1, (n, 3))
+    if n > 2:
+        pts[n // 2:] = pts[: n - n // 2]
+    dom = r.integers(0, 9, n).astype(np.int32)
+    q = r.uniform(-0.3, 1.3, (4000, 3))
+    if n:
+        q[: min(n, 100)] = pts[: min(n, 100)]
+    hp, hr = port.cp(pts, dom), ref.cp(pts, dom)
+    for thr in (float(np.finfo(np.float64).max), 0.01):
+        for x, y, what in zip(port.cp_query(hp, q, thr, threads=4), ref.cp_query(hr, q, thr, threads=4),
+                              ("index", "domain", "position", "distance")):
+            assert_bits_equal(x, y, what)
+
+
 def test_port_threads_are_deterministic(port):
     v, f = W.displaced_icosphere(3, 1)
     q = W.uniform_queries(v, 4000, 2)
