@@ -41,8 +41,8 @@ FALLBACK_HBM_GBS = 6800.0
 BATCH_MESHES = 512
 # DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) per point of one
 # k_sdf_mixed launch, measured by ncu on 1,048,576 uniform points of the same
-# mesh (1.936 GB read + 0.522 GB written); the bench scales it by its point count.
-MIXED_DRAM_BYTES_PER_POINT = (1.936470e9 + 0.522434e9) / 1048576
+# mesh (3.083 GB read + 1.237 GB written); the bench scales it by its point count.
+MIXED_DRAM_BYTES_PER_POINT = (3.083479e9 + 1.237160e9) / 1048576
 BATCH_SEED = 5
 
 
@@ -343,6 +343,41 @@ def adjoint_leg(args, G, torch):
             "deterministic": bool(torch.equal(gv.view(torch.int64), gv2.view(torch.int64)))}
 
 
+def closest_point_leg(args, G, torch, port, v, threads):
+    """DistributedClosestPoint's local query: the 655,362 vertices of the
+    level-8 mesh as object points, 16M query points uniform in the 1.2x box,
+    no threshold; both precisions, and the oracle port on a sample."""
+    from axom_gb300 import workloads as W
+    m = args.queries
+    q = torch.from_numpy(W.uniform_queries(v, m, 8)).cuda()
+    cp = G.ClosestPoint(v)
+    res = {"workload": f"{v.shape[0]} object points (the level-8 mesh vertices), {m} uniform query points"}
+    outs = {}
+    for name, prec in (("mixed", G.PRECISION_MIXED), ("fp64", G.PRECISION_FP64)):
+        for _ in range(args.warmup):
+            cp.compute_closest_points(q, precision=prec)
+        ms = []
+        for _ in range(args.steps):
+            outs[name] = cp.compute_closest_points(q, precision=prec)
+            ms.append(cp.last_query_ms())
+        res[name] = {"value": m / (statistics.median(ms) / 1000.0), "unit": UNIT, "kernel_ms": statistics.median(ms)}
+    res["mixed_equals_fp64"] = bool(all(torch.equal(a.view(torch.int32) if a.dtype == torch.int32 else
+                                                    a.view(torch.int64), b.view(torch.int32) if
+                                                    b.dtype == torch.int32 else b.view(torch.int64))
+                                        for a, b in zip(outs["mixed"], outs["fp64"])))
+    sample = q[:: max(1, m // 200_000)].cpu().numpy()
+    h = port.cp(v)
+    t0 = time.perf_counter()
+    want = port.cp_query(h, sample, threads=threads)
+    dt = time.perf_counter() - t0
+    got = outs["mixed"][0][:: max(1, m // 200_000)].cpu().numpy()
+    res["oracle_sample_equal"] = bool(np.array_equal(got, want[0]))
+    res["cpu_baseline"] = {"value": sample.shape[0] / dt, "unit": UNIT, "cores": threads, "kind": "port",
+                           "sample": f"{sample.shape[0]} of the query points"}
+    del q
+    return res
+
+
 def workload_config(args, f):
     return {"workload": f"signed distance: displaced icosphere level {LEVEL} ({f.shape[0]} triangles), "
                         f"{args.queries} uniform points in the 1.2x box per GPU",
@@ -470,6 +505,7 @@ def run_gsq(args, world, rank, local):
     if world == 1 and args.forms:
         line["near_surface"] = near_surface_leg(args, G, torch, v, f)
         line["adjoint"] = adjoint_leg(args, G, torch)
+        line["closest_point"] = closest_point_leg(args, G, torch, port, v, threads)
     if world == 1 and args.batch_meshes > 0:
         torch.cuda.empty_cache()
         line["batched"] = batched_leg(args, G, torch, lib, threads)

@@ -133,3 +133,18 @@ def test_full_size_triangle_boxes_build(gsq, port):
     tri = v[f]
     boxes = np.concatenate([tri.min(1), tri.max(1)], 1)
     check_layout(gsq, port, boxes, 1.000123)
+
+
+def test_mesh_self_query_broad_phase(gsq, port):
+    """The broad phase of MeshTester's self-intersection test
+    (quest/detail/MeshTester_detail.hpp:320-340): findBoundingBoxes with a
+    mesh's own triangle boxes as the queries (81,920 triangles, every box
+    touching its neighbours); the candidate CSR equals the oracle's."""
+    v, f = W.displaced_icosphere(6, 5)
+    tri = v[f]
+    boxes = np.concatenate([tri.min(1), tri.max(1)], 1)
+    b, h = check_layout(gsq, port, boxes, 1.000123)
+    got, want = b.find_bounding_boxes(boxes), port.find_boxes(h, boxes)
+    for x, y in zip(got, want):
+        assert_bits_equal(x, y, "self query")
+    assert int(got[1].min()) >= 1  # every box finds at least itself
