@@ -100,6 +100,7 @@ SIGNATURES = [
     ("gsq_sdf_mixed_stats", C.c_int, [_vp, _i64p]),
     ("gsq_sdf_backward", C.c_int, [_vp, _vp, _vp, _vp, C.c_int32, C.c_int32, _vp, _vp, _vp, _vp]),
     ("gsq_sdf_eval_noalloc", C.c_int, [_vp, _vp, _vp, _vp, C.c_int32, C.c_int32, _vp, _vp]),
+    ("gsq_stl_read", C.c_int, [C.c_char_p, C.POINTER(_dp), _ip, C.POINTER(_ip), _ip]),
     ("gsq_cpq_create", C.c_int, [C.POINTER(_vp), _vp, C.c_int32, _vp, _vp]),
     ("gsq_cpq_destroy", C.c_int, [_vp]),
     ("gsq_cpq_query", C.c_int, [_vp, _vp, C.c_int32, C.c_double, C.c_int32, _vp, _vp, _vp, _vp, _vp]),
@@ -298,6 +299,22 @@ class BVH:
         _check(self._lib.gsq_bvh_export(self._h, nodes.ctypes.data_as(_dp), ch.ctypes.data_as(_ip),
                                         leaf.ctypes.data_as(_ip), codes.ctypes.data_as(_up)))
         return nodes, ch, leaf, codes
+
+
+def read_stl(path) -> tuple[np.ndarray, np.ndarray]:
+    """quest::STLReader (quest/readers/STLReader.cpp): (nodes (n, 3), triangles
+    (n/3, 3)) of an ASCII or binary STL file, three nodes per triangle."""
+    lib = load()
+    xyz, cells = _dp(), _ip()
+    nn, nc = C.c_int32(), C.c_int32()
+    _check(lib.gsq_stl_read(str(path).encode(), C.byref(xyz), C.byref(nn), C.byref(cells), C.byref(nc)))
+    try:
+        v = np.ctypeslib.as_array(xyz, shape=(max(nn.value, 1) * 3,))[: 3 * nn.value].reshape(-1, 3).copy()
+        f = np.ctypeslib.as_array(cells, shape=(max(nc.value, 1) * 3,))[: 3 * nc.value].reshape(-1, 3).copy()
+    finally:
+        lib.gsq_free(xyz)
+        lib.gsq_free(cells)
+    return v, f
 
 
 def normalize_rays(directions) -> np.ndarray:

@@ -233,6 +233,18 @@ int gsq_sdf_backward(const gsq_sdf* sdf, const double* qx, const double* qy, con
  * No reference counterpart (the reference has only the FP64 form). */
 int gsq_sdf_mixed_stats(const gsq_sdf* sdf, int64_t* counters);
 
+/* ---- Surface-mesh input --------------------------------------------------
+ * Replaces quest::STLReader::read + getMesh (quest/readers/STLReader.cpp) as
+ * used by signed_distance_init(file) (quest/interface/internal/
+ * QuestHelpers.cpp:287-320): reads an ASCII or binary STL file (binary iff the
+ * file size is 84 + 50 n for the triangle count n in its header).  Every
+ * triangle gets its own three nodes in file order (no merging, as the
+ * reference); cell i is (3i, 3i+1, 3i+2).  Host arrays, freed with gsq_free:
+ *   xyz    nnodes x 3 coordinates (AoS)
+ *   cells  ncells x 3 node ids
+ * The mesh feeds gsq_sdf_create with stride-3 coordinate pointers. */
+int gsq_stl_read(const char* path, double** xyz, int32_t* nnodes, int32_t** cells, int32_t* ncells);
+
 /* ---- Closest object point ----------------------------------------------
  * Replaces the local step of quest::DistributedClosestPoint
  * (quest/detail/DistributedClosestPointImpl.hpp: generateBVHTreeImpl 883-901,

@@ -260,6 +260,20 @@ class Ref(_Lib):
                                     int(watertight), int(compute_sign))
         return _Handle(self, h, "sdf_destroy")
 
+    def stl_read(self, path):
+        """quest::STLReader::read + getMesh: (nodes (n, 3), triangles (n/3, 3)), or None if read() failed."""
+        fn = self.lib.ref_stl_read
+        fn.restype, fn.argtypes = C.c_int, [C.c_char_p, C.POINTER(_dp), _ip, C.POINTER(_ip)]
+        xyz, conn, nn = _dp(), _ip(), C.c_int()
+        nc = fn(str(path).encode(), C.byref(xyz), C.byref(nn), C.byref(conn))
+        if nc < 0:
+            return None
+        v = np.ctypeslib.as_array(xyz, shape=(max(nn.value, 1) * 3,))[: 3 * nn.value].reshape(-1, 3).copy()
+        f = np.ctypeslib.as_array(conn, shape=(max(nc, 1) * 3,))[: 3 * nc].reshape(-1, 3).copy()
+        self.lib.ref_free(xyz)
+        self.lib.ref_free(conn)
+        return v, f
+
     def find_rays(self, h, o, d_raw):
         """Rays built by primal::Ray(o, d): returns (off, cnt, cand, stored unit dirs)."""
         o = _arr(o, np.float64).reshape(-1, 3)

@@ -63,6 +63,7 @@ SOURCES = [
     "axom/mint/utils/vtk_utils.cpp",
     "axom/mint/fem/FiniteElement.cpp",
     "axom/quest/SignedDistance.cpp",
+    "axom/quest/readers/STLReader.cpp",
 ]
 
 ENABLED = {

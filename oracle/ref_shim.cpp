@@ -20,6 +20,7 @@
 #include "axom/spin/BVH.hpp"
 #include "axom/spin/internal/linear_bvh/build_radix_tree.hpp"
 #include "axom/quest/SignedDistance.hpp"
+#include "axom/quest/readers/STLReader.hpp"
 
 #include <cstdint>
 #include <cstdlib>
@@ -311,6 +312,36 @@ void ref_sdf_mesh_bounds(void* hv, double* out6)
   BoxType bb;
   for(size_t i = 0; i < h->x.size(); ++i) bb.addPoint(PointType {h->x[i], h->y[i], h->z[i]});
   put_box(bb, out6);
+}
+
+// ---- quest::STLReader (quest/readers/STLReader.cpp) --------------------------
+// Reads the file and copies the mesh STLReader::getMesh builds: coordinates
+// (AoS, 3 per node) and connectivity (3 per triangle).  Returns the number of
+// triangles, or -1 if read() failed; the arrays are malloc'd (ref_free).
+int ref_stl_read(const char* path, double** xyz, int* nnodes, int** conn)
+{
+  ensure_logger();
+  axom::quest::STLReader reader;
+  reader.setFileName(path);
+  if(reader.read() != 0) return -1;
+  UMesh mesh(3, axom::mint::TRIANGLE);
+  reader.getMesh(&mesh);
+  const int nn = (int)mesh.getNumberOfNodes(), nc = (int)mesh.getNumberOfCells();
+  *nnodes = nn;
+  *xyz = static_cast<double*>(std::malloc(sizeof(double) * 3 * std::max(nn, 1)));
+  *conn = static_cast<int*>(std::malloc(sizeof(int) * 3 * std::max(nc, 1)));
+  const double* x = mesh.getCoordinateArray(axom::mint::X_COORDINATE);
+  const double* y = mesh.getCoordinateArray(axom::mint::Y_COORDINATE);
+  const double* z = mesh.getCoordinateArray(axom::mint::Z_COORDINATE);
+  for(int i = 0; i < nn; ++i)
+  {
+    (*xyz)[3 * i] = x[i];
+    (*xyz)[3 * i + 1] = y[i];
+    (*xyz)[3 * i + 2] = z[i];
+  }
+  const axom::IndexType* c = mesh.getCellNodesArray();
+  for(int i = 0; i < 3 * nc; ++i) (*conn)[i] = (int)c[i];
+  return nc;
 }
 
 // ---- the local closest-point query of quest::DistributedClosestPoint --------
