@@ -57,6 +57,12 @@ class SdfOpts(C.Structure):
                 ("audit", C.c_int32), ("queue_depth", C.c_int32), ("reserved", C.c_int32 * 3)]
 
 
+class BvhView(C.Structure):
+    """gsq_bvh_view: device pointers for user kernels (include/gsq_device.cuh)."""
+    _fields_ = [("nodes", C.c_void_p), ("leaf_ids", C.c_void_p), ("num_leaves", C.c_int32),
+                ("reserved", C.c_int32)]
+
+
 class BatchOpts(C.Structure):
     _fields_ = [("block_size", C.c_int32), ("queue_depth", C.c_int32), ("stack_depth", C.c_int32),
                 ("morton_bits", C.c_int32), ("leaf_size", C.c_int32), ("closest_points", C.c_int32),
@@ -101,6 +107,7 @@ SIGNATURES = [
     ("gsq_sdf_backward", C.c_int, [_vp, _vp, _vp, _vp, C.c_int32, C.c_int32, _vp, _vp, _vp, _vp]),
     ("gsq_sdf_eval_noalloc", C.c_int, [_vp, _vp, _vp, _vp, C.c_int32, C.c_int32, _vp, _vp]),
     ("gsq_stl_read", C.c_int, [C.c_char_p, C.POINTER(_dp), _ip, C.POINTER(_ip), _ip]),
+    ("gsq_bvh_get_view", C.c_int, [_vp, C.POINTER(BvhView)]),
     ("gsq_cpq_create", C.c_int, [C.POINTER(_vp), _vp, C.c_int32, _vp, _vp]),
     ("gsq_cpq_destroy", C.c_int, [_vp]),
     ("gsq_cpq_query", C.c_int, [_vp, _vp, C.c_int32, C.c_double, C.c_int32, _vp, _vp, _vp, _vp, _vp]),
@@ -252,6 +259,12 @@ class BVH:
         v = C.c_float()
         _check(self._lib.gsq_bvh_last_build_ms(self._h, C.byref(v)))
         return v.value
+
+    def get_view(self) -> BvhView:
+        """BVH::getTraverser: device pointers for user kernels (include/gsq_device.cuh)."""
+        v = BvhView()
+        _check(self._lib.gsq_bvh_get_view(self._h, C.byref(v)))
+        return v
 
     def _find(self, fn, arrs, m, like: _Arr):
         off = like.empty(m, np.int32)

@@ -729,6 +729,18 @@ int gsq_bvh_find_rays(const gsq_bvh* h, const double* o, const double* d, int32_
   return find_impl<Q_RAYS>(h, o, d, m, offsets, counts, candidates, total, stream);
 }
 
+int gsq_bvh_get_view(const gsq_bvh* h, gsq_bvh_view* view)
+{
+  int rc = check_bvh(h);
+  if(rc) return rc;
+  if(!view) return fail(GSQ_ERR_INVALID, "null view");
+  view->nodes = h->dev.nodes;
+  view->leaf_ids = h->dev.perm;
+  view->num_leaves = h->dev.n;
+  view->reserved = 0;
+  return GSQ_OK;
+}
+
 int gsq_bvh_export(const gsq_bvh* h, double* node_boxes, int32_t* children, int32_t* leaf_ids, uint32_t* codes)
 {
   int rc = check_bvh(h);

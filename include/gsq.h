@@ -130,6 +130,19 @@ int gsq_ray_normalize(const double* raw, int32_t m, double* unit);
 int gsq_bvh_export(const gsq_bvh* bvh, double* node_boxes, int32_t* children, int32_t* leaf_ids,
                    uint32_t* codes);
 
+/* Replaces BVH::getTraverser (spin/BVH.hpp:319): device pointers to the built
+ * tree for user kernels, traversed with gsq::device::traverse_tree
+ * (include/gsq_device.cuh).  Valid until the next build or destroy.
+ *   nodes      num_leaves - 1 node records of 128 bytes (gsq::device::Node)
+ *   leaf_ids   num_leaves original box ids, by sorted leaf position */
+typedef struct gsq_bvh_view {
+  const void* nodes;
+  const int32_t* leaf_ids;
+  int32_t num_leaves;
+  int32_t reserved;
+} gsq_bvh_view;
+int gsq_bvh_get_view(const gsq_bvh* bvh, gsq_bvh_view* view);
+
 /* Milliseconds of device time taken by the last gsq_bvh_build on this
  * handle (CUDA events around the build's kernels). */
 int gsq_bvh_last_build_ms(const gsq_bvh* bvh, float* ms);
