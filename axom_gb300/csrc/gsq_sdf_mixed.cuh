@@ -97,6 +97,57 @@ __device__ __forceinline__ float dist2_f32(const float* P, const float* A, const
              __fmaf_rn(-w, ac2, __fmaf_rn(-v, ab2, ap2)));
 }
 
+// True when every fuzzy comparison of the reference's closest_point
+// (closest_point.hpp:181-282: d1..d6, d4 - d3, d5 - d6, d1 - d3 and vc, vb, va
+// against 0 with EPS = 1e-12) certainly has the outcome of the exact
+// comparison.  The reference's point is then the exact closest point up to
+// FP64 rounding, and its fuzzy displacement bound is not needed.
+//   u  bounds the error of every FP32 coordinate difference against the exact
+//      one: the vertices and the point are rounded to FP32 (2^-24 M, 2^-24 |q|)
+//      and the difference once more, so u = 2^-22 (|q| + M) covers all three.
+// A dot product of differences e, p is then within
+//   err_d = u (|e|_1 + |p|_1 + 6u) + 3u^2 + 2^-23 |e|_1 |p|_1
+// of the exact one (the last term: the fused dot's own rounding), a product
+// difference a b - c d within 4 D err_d + 2 err_d^2 + 2^-22 D^2 (D the largest
+// |d| plus err_d), a difference of two dots within 2 err_d + 2^-23 D.  Each
+// value must exceed twice its bound plus 2 EPS: then the FP64 value, whose own
+// rounding error is below 2^-28 of the FP32 bound, is beyond EPS with the
+// exact value's sign.
+__device__ __forceinline__ bool crisp_regions(const float* P, const float* A, const float* B, const float* C, float u)
+{
+  constexpr float EPS = 1e-12f;
+  const float ab0 = B[0] - A[0], ab1 = B[1] - A[1], ab2 = B[2] - A[2];
+  const float ac0 = C[0] - A[0], ac1 = C[1] - A[1], ac2 = C[2] - A[2];
+  const float ap0 = P[0] - A[0], ap1 = P[1] - A[1], ap2 = P[2] - A[2];
+  const float bp0 = P[0] - B[0], bp1 = P[1] - B[1], bp2 = P[2] - B[2];
+  const float cp0 = P[0] - C[0], cp1 = P[1] - C[1], cp2 = P[2] - C[2];
+  const float d1 = dot3f(ab0, ap0, ab1, ap1, ab2, ap2);
+  const float d2 = dot3f(ac0, ap0, ac1, ap1, ac2, ap2);
+  const float d3 = dot3f(ab0, bp0, ab1, bp1, ab2, bp2);
+  const float d4 = dot3f(ac0, bp0, ac1, bp1, ac2, bp2);
+  const float d5 = dot3f(ab0, cp0, ab1, cp1, ab2, cp2);
+  const float d6 = dot3f(ac0, cp0, ac1, cp1, ac2, cp2);
+  const float vc = __fmaf_rn(d1, d4, -(d3 * d2));
+  const float vb = __fmaf_rn(d5, d2, -(d1 * d6));
+  const float va = __fmaf_rn(d3, d6, -(d5 * d4));
+  auto n1 = [](float x, float y, float z) { return fabsf(x) + fabsf(y) + fabsf(z); };
+  const float E1 = fmaxf(n1(ab0, ab1, ab2), n1(ac0, ac1, ac2));
+  const float P1 = fmaxf(n1(ap0, ap1, ap2), fmaxf(n1(bp0, bp1, bp2), n1(cp0, cp1, cp2)));
+  const float err_d = __fmul_ru(1.01f, __fadd_ru(__fadd_ru(__fmul_ru(u, __fadd_ru(__fadd_ru(E1, P1), 6.f * u)),
+                                                           3.f * u * u),
+                                                  __fmul_ru(0x1p-23f, __fmul_ru(E1, P1))));
+  const float D = __fadd_ru(fmaxf(fmaxf(fmaxf(fabsf(d1), fabsf(d2)), fmaxf(fabsf(d3), fabsf(d4))),
+                                  fmaxf(fabsf(d5), fabsf(d6))),
+                            err_d);
+  const float err_v = __fmul_ru(1.01f, __fadd_ru(__fadd_ru(__fmul_ru(4.f * D, err_d), 2.f * err_d * err_d),
+                                                 __fmul_ru(0x1p-22f, __fmul_ru(D, D))));
+  const float err_s = __fmul_ru(1.01f, __fadd_ru(2.f * err_d, __fmul_ru(0x1p-23f, D)));
+  auto clear = [&](float x, float e) { return fabsf(x) > __fadd_ru(2.f * e, 2.f * EPS); };
+  return clear(d1, err_d) && clear(d2, err_d) && clear(d3, err_d) && clear(d4, err_d) && clear(d5, err_d) &&
+         clear(d6, err_d) && clear(d4 - d3, err_s) && clear(d5 - d6, err_s) && clear(d1 - d3, err_s) &&
+         clear(vc, err_v) && clear(vb, err_v) && clear(va, err_v);
+}
+
 // dist2_f32 without branches: the same region tests in the same order and the
 // same formulas per region, selected instead of branched to, so that the
 // lanes of a warp testing different triangles do not diverge.  One division
@@ -356,6 +407,8 @@ __device__ __forceinline__ int leaf_prefilter_bounds(const LeafRec32<NPC>* __res
         const float kl = __fdiv_ru(kappa, lt[s]);
         fz = __fmul_ru(2e-12f, __fadd_ru(kl, __fdiv_ru(__fmul_ru(kl, kl), lt[s])));
       }
+      // no fuzzy displacement when every region test is clear of its EPS band
+      if(crisp_regions(c.qf, A, B, C, 0.5f * c.lip)) fz = 0.f;
       // sqrt(d2 (1 -+ 2^-20)) from the correctly rounded sqrt(d2): the factor
       // 1 -+ 2^-20 covers both the 2^-21 of the square root of the margin and
       // the 2^-24 rounding of sqrtf

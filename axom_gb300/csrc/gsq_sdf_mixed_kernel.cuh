@@ -36,7 +36,7 @@ struct MixedStats
 // tree is shallow enough).  MULTI: the points belong to several meshes (point
 // ranges qoff[k].. of mesh k, whose records start at meshes[k]'s offsets);
 // otherwise to the one mesh meshes[0] with its node box in prm_all.
-constexpr int BATCH_MIN = 20;
+constexpr int BATCH_MIN = 16;
 
 template <int NPC, bool AUDIT, int QCAP, int STK, bool MULTI>
 __global__ void __launch_bounds__(128, 5) k_sdf_mixed(const NodeRec64* __restrict__ nodes64_all,
