@@ -11,6 +11,7 @@
 #ifndef GSQ_HPP_
 #define GSQ_HPP_
 
+#include <cfloat>
 #include <cstdint>
 #include <stdexcept>
 #include <string>
@@ -234,6 +235,70 @@ public:
 
 private:
   gsq_sdf* m_h = nullptr;
+};
+
+// STLReader (quest/readers/STLReader.hpp): setFileName, read, getMesh.
+class STLReader
+{
+public:
+  void setFileName(const std::string& name) { m_file = name; }
+  // read() (STLReader.cpp:190-202): 0 on success, -1 otherwise
+  int read()
+  {
+    double* xyz = nullptr;
+    int32_t* cells = nullptr;
+    int32_t nn = 0, nc = 0;
+    if(gsq_stl_read(m_file.c_str(), &xyz, &nn, &cells, &nc) != GSQ_OK) return -1;
+    m_mesh.x.resize(nn);
+    m_mesh.y.resize(nn);
+    m_mesh.z.resize(nn);
+    for(int32_t i = 0; i < nn; ++i)
+    {
+      m_mesh.x[i] = xyz[3 * i];
+      m_mesh.y[i] = xyz[3 * i + 1];
+      m_mesh.z[i] = xyz[3 * i + 2];
+    }
+    m_mesh.cells.assign(cells, cells + 3 * (size_t)nc);
+    m_mesh.nodes_per_cell = 3;
+    gsq_free(xyz);
+    gsq_free(cells);
+    return 0;
+  }
+  // getMesh (STLReader.cpp:205-250): three nodes per triangle, in file order
+  void getMesh(SurfaceMesh& mesh) const { mesh = m_mesh; }
+
+private:
+  std::string m_file;
+  SurfaceMesh m_mesh;
+};
+
+// The local step of DistributedClosestPoint
+// (quest/detail/DistributedClosestPointImpl.hpp:883-901, 1002-1050).
+class ClosestPoint
+{
+public:
+  // the object points (generateBVHTree) and their domain ids (nullable)
+  ClosestPoint(int32_t n, const Point* pts, const int32_t* domain_ids = nullptr, void* stream = nullptr)
+  {
+    check(gsq_cpq_create(&m_h, reinterpret_cast<const double*>(pts), n, domain_ids, stream));
+  }
+  ~ClosestPoint() { gsq_cpq_destroy(m_h); }
+  ClosestPoint(const ClosestPoint&) = delete;
+  ClosestPoint& operator=(const ClosestPoint&) = delete;
+  // setDistanceThreshold (DistributedClosestPoint.cpp:125-130) stores t * t
+  void setDistanceThreshold(double t) { m_sq_threshold = t * t; }
+  // per query point: closest object point index and domain (-1 if none),
+  // its coordinates and distance (NaN if none)
+  void computeClosestPoints(int32_t m, const Point* queries, int32_t* idx, int32_t* dom, Point* pos, double* dist,
+                            int32_t precision = GSQ_PRECISION_MIXED, void* stream = nullptr) const
+  {
+    check(gsq_cpq_query(m_h, reinterpret_cast<const double*>(queries), m, m_sq_threshold, precision, idx, dom,
+                        reinterpret_cast<double*>(pos), dist, stream));
+  }
+
+private:
+  gsq_cpq* m_h = nullptr;
+  double m_sq_threshold = DBL_MAX;
 };
 }  // namespace quest
 }  // namespace gsq

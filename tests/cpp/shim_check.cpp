@@ -62,6 +62,56 @@ int main()
           EXPECT(std::fabs(d - p.x[2]) <= 4 * 2.220446049250313e-16 * std::fabs(p.x[2]));
         }
   }
+  // STL round trip: the plane's four triangles as an ASCII file, read back
+  // through the reader and evaluated like the mesh above
+  {
+    const char* path = "shim_check_plane.stl";
+    FILE* f = std::fopen(path, "w");
+    EXPECT(f != nullptr);
+    std::fprintf(f, "solid plane\n");
+    for(size_t t = 0; t < plane.cells.size(); t += 3)
+    {
+      std::fprintf(f, "facet normal 0 0 1\nouter loop\n");
+      for(int k = 0; k < 3; ++k)
+      {
+        const int v = plane.cells[t + k];
+        std::fprintf(f, "vertex %.17g %.17g %.17g\n", plane.x[v], plane.y[v], plane.z[v]);
+      }
+      std::fprintf(f, "endloop\nendfacet\n");
+    }
+    std::fprintf(f, "endsolid plane\n");
+    std::fclose(f);
+    gsq::quest::STLReader reader;
+    reader.setFileName(path);
+    EXPECT(reader.read() == 0);
+    gsq::quest::SurfaceMesh m;
+    reader.getMesh(m);
+    EXPECT(m.x.size() == 12 && m.numCells() == 4);
+    gsq::quest::SignedDistance<3> sd(m, false);
+    const gsq::Point p {{0.5, -1.25, 2.0}};
+    EXPECT(std::fabs(sd.computeDistance(p) - 2.0) <= 1e-15);
+    std::remove(path);
+  }
+
+  // closest object point: the 27 cell corners (0..3)^3 minus one
+  {
+    std::vector<gsq::Point> pts;
+    for(int k = 0; k < 4; ++k)
+      for(int j = 0; j < 4; ++j)
+        for(int i = 0; i < 4; ++i) pts.push_back({{double(i), double(j), double(k)}});
+    gsq::quest::ClosestPoint cp((int32_t)pts.size(), pts.data());
+    const gsq::Point qs[2] = {{{1.1, 2.2, 2.9}}, {{10.0, 10.0, 10.0}}};
+    int32_t idx[2], dom[2];
+    gsq::Point pos[2];
+    double dist[2];
+    cp.computeClosestPoints(2, qs, idx, dom, pos, dist);
+    EXPECT(idx[0] == 1 + 4 * 2 + 16 * 3 && dom[0] == 0);
+    EXPECT(pos[0].x[0] == 1.0 && pos[0].x[1] == 2.0 && pos[0].x[2] == 3.0);
+    cp.setDistanceThreshold(1.0);
+    cp.computeClosestPoints(2, qs, idx, dom, pos, dist);
+    EXPECT(idx[0] >= 0 && idx[1] == -1 && dist[1] != dist[1]);
+  }
+
   std::printf("%s (%d failures)\n", failures ? "FAIL" : "OK", failures);
   return failures ? 1 : 0;
 }

@@ -17,6 +17,6 @@ def test_cpp_shim_known_answers(gsq, tmp_path):
     lib_dir = ROOT / "axom_gb300"
     subprocess.run(["g++", "-std=c++17", "-O2", f"-I{ROOT / 'include'}", str(ROOT / "tests/cpp/shim_check.cpp"),
                     f"-L{lib_dir}", "-lgsq", f"-Wl,-rpath,{lib_dir}", "-o", str(exe)], check=True)
-    p = subprocess.run([str(exe)], capture_output=True, text=True, timeout=120)
+    p = subprocess.run([str(exe)], capture_output=True, text=True, timeout=120, cwd=tmp_path)
     assert p.returncode == 0, p.stdout + p.stderr
     assert "OK" in p.stdout
