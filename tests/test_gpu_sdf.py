@@ -7,6 +7,7 @@ from __future__ import annotations
 import numpy as np
 import pytest
 
+import axom_gb300
 from axom_gb300 import workloads as W
 from conftest import assert_bits_equal, golden
 
@@ -82,14 +83,17 @@ def test_tiny_meshes(gsq, port):
     """0, 1 and 2 triangles (BVH padding), one point query far away and near."""
     v = np.array([[0.0, 0, 0], [1, 0, 0], [0, 1, 0], [1, 1, 0.5]])
     q = np.array([[0.2, 0.2, 0.3], [5.0, -3, 2], [0.5, 0.5, -0.1], [0.0, 0.0, 0.0]])
-    for f in (np.array([[0, 1, 2]], np.int32), np.array([[0, 1, 2], [1, 3, 2]], np.int32)):
+    for f in (np.zeros((0, 3), np.int32), np.array([[0, 1, 2]], np.int32),
+              np.array([[0, 1, 2], [1, 3, 2]], np.int32)):
         for wt in (True, False):
-            sd = gsq.SignedDistance(v, f, is_watertight=wt)
             h = port.sdf(v[:, 0], v[:, 1], v[:, 2], f, wt, True)
-            d, cp, _ = sd.compute_distances(q, closest=True, normals=True)
             pd, pcp, _ = port.sdf_eval(h, q, True, True)
-            assert_bits_equal(d, pd, "distance")
-            assert_bits_equal(cp, pcp, "closest")
+            for precision in (axom_gb300.PRECISION_FP64, axom_gb300.PRECISION_MIXED):
+                sd = gsq.SignedDistance(v, f, is_watertight=wt, precision=precision)
+                d, cp, _ = sd.compute_distances(q, closest=True, normals=True)
+                assert_bits_equal(d, pd, "distance")
+                assert_bits_equal(cp, pcp, "closest")
+                assert sd.compute_distances(q[:0]).shape == (0,)  # no points
 
 
 def test_full_size_sample(gsq, port):
