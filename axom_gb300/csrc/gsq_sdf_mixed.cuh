@@ -43,58 +43,12 @@ struct MeshInfo
 
 namespace sdf
 {
-// Squared point-triangle distance in FP32 by Voronoi regions (Ericson,
-// Real-Time Collision Detection 5.1.5), measured from P.  off (optional)
-// receives P - cp, the offset from the closest point.  Products are fused
-// (one rounding per multiply-add): the error bounds used with this function
-// count at least one rounding per operation, which fused operations meet.
+// FP32 dot product with fused operations (one rounding per multiply-add):
+// the error bounds used with these FP32 evaluations count at least one
+// rounding per operation, which fused operations meet.
 __device__ __forceinline__ float dot3f(float a0, float b0, float a1, float b1, float a2, float b2)
 {
   return __fmaf_rn(a2, b2, __fmaf_rn(a1, b1, a0 * b0));
-}
-__device__ __forceinline__ float dist2_f32(const float* P, const float* A, const float* B, const float* C,
-                                          float* off = nullptr)
-{
-  auto ret = [&](float x, float y, float z) {
-    if(off) off[0] = x, off[1] = y, off[2] = z;
-    return dot3f(x, x, y, y, z, z);
-  };
-  const float ab0 = B[0] - A[0], ab1 = B[1] - A[1], ab2 = B[2] - A[2];
-  const float ac0 = C[0] - A[0], ac1 = C[1] - A[1], ac2 = C[2] - A[2];
-  const float ap0 = P[0] - A[0], ap1 = P[1] - A[1], ap2 = P[2] - A[2];
-  const float d1 = dot3f(ab0, ap0, ab1, ap1, ab2, ap2);
-  const float d2 = dot3f(ac0, ap0, ac1, ap1, ac2, ap2);
-  if(d1 <= 0.f && d2 <= 0.f) return ret(ap0, ap1, ap2);
-  const float bp0 = P[0] - B[0], bp1 = P[1] - B[1], bp2 = P[2] - B[2];
-  const float d3 = dot3f(ab0, bp0, ab1, bp1, ab2, bp2);
-  const float d4 = dot3f(ac0, bp0, ac1, bp1, ac2, bp2);
-  if(d3 >= 0.f && d4 <= d3) return ret(bp0, bp1, bp2);
-  const float vc = __fmaf_rn(d1, d4, -(d3 * d2));
-  if(vc <= 0.f && d1 >= 0.f && d3 <= 0.f)
-  {
-    const float v = d1 / (d1 - d3);
-    return ret(__fmaf_rn(-v, ab0, ap0), __fmaf_rn(-v, ab1, ap1), __fmaf_rn(-v, ab2, ap2));
-  }
-  const float cp0 = P[0] - C[0], cp1 = P[1] - C[1], cp2 = P[2] - C[2];
-  const float d5 = dot3f(ab0, cp0, ab1, cp1, ab2, cp2);
-  const float d6 = dot3f(ac0, cp0, ac1, cp1, ac2, cp2);
-  if(d6 >= 0.f && d5 <= d6) return ret(cp0, cp1, cp2);
-  const float vb = __fmaf_rn(d5, d2, -(d1 * d6));
-  if(vb <= 0.f && d2 >= 0.f && d6 <= 0.f)
-  {
-    const float w = d2 / (d2 - d6);
-    return ret(__fmaf_rn(-w, ac0, ap0), __fmaf_rn(-w, ac1, ap1), __fmaf_rn(-w, ac2, ap2));
-  }
-  const float va = __fmaf_rn(d3, d6, -(d5 * d4));
-  if(va <= 0.f && (d4 - d3) >= 0.f && (d5 - d6) >= 0.f)
-  {
-    const float w = (d4 - d3) / ((d4 - d3) + (d5 - d6));
-    return ret(bp0 - w * (C[0] - B[0]), bp1 - w * (C[1] - B[1]), bp2 - w * (C[2] - B[2]));
-  }
-  const float denom = 1.f / (va + vb + vc);
-  const float v = vb * denom, w = vc * denom;
-  return ret(__fmaf_rn(-w, ac0, __fmaf_rn(-v, ab0, ap0)), __fmaf_rn(-w, ac1, __fmaf_rn(-v, ab1, ap1)),
-             __fmaf_rn(-w, ac2, __fmaf_rn(-v, ab2, ap2)));
 }
 
 // True when every fuzzy comparison of the reference's closest_point
@@ -148,11 +102,13 @@ __device__ __forceinline__ bool crisp_regions(const float* P, const float* A, co
          clear(vc, err_v) && clear(vb, err_v) && clear(va, err_v);
 }
 
-// dist2_f32 without branches: the same region tests in the same order and the
-// same formulas per region, selected instead of branched to, so that the
-// lanes of a warp testing different triangles do not diverge.  One division
-// serves every region (its operands are selected); the offset is
-// base - v e1 - w e2 with fused operations.
+// Squared point-triangle distance in FP32 by Voronoi regions (Ericson,
+// Real-Time Collision Detection 5.1.5), measured from P; off receives P - cp,
+// the offset from the closest point.  The region tests run in Ericson's order
+// and each region keeps its formula, but the results are selected instead of
+// branched to, so that the lanes of a warp testing different triangles do not
+// diverge.  One division serves every region (its operands are selected); the
+// offset is base - v e1 - w e2 with fused operations.
 __device__ __forceinline__ float dist2_f32_flat(const float* P, const float* A, const float* B, const float* C,
                                                float* off)
 {
@@ -340,7 +296,8 @@ __device__ __forceinline__ int leaf_prefilter(const LeafRec32<NPC>* __restrict__
     const float* A = v;
     const float* B = v + 3 * (s + 1);
     const float* C = v + 3 * (s + 2);
-    const float d2 = dist2_f32(c.qf, A, B, C);
+    float off[3];
+    const float d2 = dist2_f32_flat(c.qf, A, B, C, off);
     const float ap = fmaxf(fabsf(c.qf[0] - A[0]), fmaxf(fabsf(c.qf[1] - A[1]), fabsf(c.qf[2] - A[2])));
     const float E = __fadd_ru(c.lip, __fmul_ru(ec[s], __fadd_ru(ap, lt[s])));
     const float lim = __fadd_ru(c.thr_leaf, E);

@@ -19,8 +19,9 @@ struct MixedStats
 };
 
 // Persistent warp loop over a work queue of Morton-ordered points.  Each lane
-// runs one point's traversal as a resumable state machine, one FP32 step per
-// iteration.  Leaves that the FP32 certificate cannot skip are queued (up to
+// runs one point's traversal as a resumable state machine; an iteration takes
+// the deferred leaf where the descent stopped (if any), then one node visit,
+// both decided in FP32.  Leaves that the FP32 certificate cannot skip are queued (up to
 // QCAP per lane) instead of being refined at once: until they are refined the
 // exact running minimum is only known to lie in an interval (the resolved
 // minimum and certified bounds of the queued candidates' FP64 distances), and
