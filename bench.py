@@ -500,7 +500,7 @@ def run_gsq(args, world, rank, local):
         "gpu_launches": int(launches),
         "clocks": clk,
     }
-    if not args.no_cpu_baseline:
+    if world == 1 and not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline(port, v, f, q_host, args.cpu_seconds, threads)
     if world == 1 and args.forms:
         line["near_surface"] = near_surface_leg(args, G, torch, v, f)
