@@ -108,9 +108,10 @@ __device__ __forceinline__ bool crisp_regions(const float* P, const float* A, co
 // and each region keeps its formula, but the results are selected instead of
 // branched to, so that the lanes of a warp testing different triangles do not
 // diverge.  One division serves every region (its operands are selected); the
-// offset is base - v e1 - w e2 with fused operations.
+// offset is base - v e1 - w e2 with fused operations.  kind receives the
+// region: 0 a vertex, 1 the edge AB or AC, 2 the edge BC or the face.
 __device__ __forceinline__ float dist2_f32_flat(const float* P, const float* A, const float* B, const float* C,
-                                               float* off)
+                                               float* off, int& kind)
 {
   const float ab0 = B[0] - A[0], ab1 = B[1] - A[1], ab2 = B[2] - A[2];
   const float ac0 = C[0] - A[0], ac1 = C[1] - A[1], ac2 = C[2] - A[2];
@@ -134,6 +135,7 @@ __device__ __forceinline__ float dist2_f32_flat(const float* P, const float* A, 
   const bool rAC = !rA && !rB && !rAB && !rC && vb <= 0.f && d2 >= 0.f && d6 <= 0.f;
   const bool rBC = !rA && !rB && !rAB && !rC && !rAC && va <= 0.f && (d4 - d3) >= 0.f && (d5 - d6) >= 0.f;
   const bool rF = !rA && !rB && !rAB && !rC && !rAC && !rBC;
+  kind = (rA || rB || rC) ? 0 : (rAB || rAC) ? 1 : 2;
   const float num = rAB ? d1 : rAC ? d2 : rBC ? (d4 - d3) : 1.f;
   const float den = rAB ? (d1 - d3) : rAC ? (d2 - d6) : rBC ? ((d4 - d3) + (d5 - d6)) : rF ? (va + vb + vc) : 1.f;
   const float t = num / den;
@@ -235,10 +237,10 @@ __device__ __forceinline__ bool visit32(const NodeRec32* __restrict__ nodes32, i
   const float lo_l[3] = {a.x, a.y, a.z}, hi_l[3] = {a.w, b.x, b.y};
   const float lo_r[3] = {b.z, b.w, cc.x}, hi_r[3] = {cc.y, cc.z, cc.w};
   const float sl_ = __int_as_float(lk.z), sr_ = __int_as_float(lk.w);
-  const bool vl = lo_l[0] <= hi_l[0] && lo_l[1] <= hi_l[1] && lo_l[2] <= hi_l[2];
-  const bool vr = lo_r[0] <= hi_r[0] && lo_r[1] <= hi_r[1] && lo_r[2] <= hi_r[2];
-  const int dl = vl ? box_decide(lo_l, hi_l, sl_, c) : 0;
-  const int dr = vr ? box_decide(lo_r, hi_r, sr_, c) : 0;
+  // an invalid box is stored as [+inf, -inf]: its gap is +inf, box_decide
+  // leaves it undecided and the FP64 visit applies the validity rule
+  const int dl = box_decide(lo_l, hi_l, sl_, c);
+  const int dr = box_decide(lo_r, hi_r, sr_, c);
   if(dl == 2 || dr == 2) return false;
   swap = false;
   if(dl == 1 && dr == 1)
@@ -297,13 +299,41 @@ __device__ __forceinline__ int leaf_prefilter(const LeafRec32<NPC>* __restrict__
     const float* B = v + 3 * (s + 1);
     const float* C = v + 3 * (s + 2);
     float off[3];
-    const float d2 = dist2_f32_flat(c.qf, A, B, C, off);
+    int kind;
+    const float d2 = dist2_f32_flat(c.qf, A, B, C, off, kind);
     const float ap = fmaxf(fabsf(c.qf[0] - A[0]), fmaxf(fabsf(c.qf[1] - A[1]), fabsf(c.qf[2] - A[2])));
     const float E = __fadd_ru(c.lip, __fmul_ru(ec[s], __fadd_ru(ap, lt[s])));
     const float lim = __fadd_ru(c.thr_leaf, E);
     if(!(d2 > __fmul_ru(__fmul_ru(lim, lim), 1.0f + 0x1p-20f))) need |= 1 << s;
   }
   return need;
+}
+
+// Error of the FP32 distance sqrt(d2) = sd of dist2_f32_flat when its region
+// is certain (crisp_regions) and not the edge BC or the face.  u = 2^-24.
+// Rounding the point and the vertices moves the exact distance by at most
+// u sqrt(3) (|q|_inf + M) (it is 1-Lipschitz in them), below lip / 4.
+//  * vertex V: off = fl(qf - Vf) exactly as the offset, within u |off| of
+//    qf - Vf: sd is within lip / 4 + 2^-23 sd of |q - V|, and the FP64 point
+//    is V itself;
+//  * edge AB (AC alike): t = d1 / (d1 - d3) and off = fl(ap - t ab).  With
+//    dots of rounded differences within 5.01 u |e| |p| of the exact ones,
+//    |t - t*| <= 5.1 u (2 |ap| + |bp|) / |ab| + 2 u to first order, and
+//    |off - off*| <= u (|off| + 16.3 |ap|_2 + 8.1 |ab|) with |ap|_2 <=
+//    sqrt(3) ap (ap the largest coordinate of qf - A) and |ab| <= lt:
+//    lip / 4 + 2^-23 sd + 2^-19 ap + 2^-20 lt.  First order holds while the
+//    relative error of d1 - d3 is small: every edge is at least lt / kappa
+//    long (kappa = ec 2^16), so ap ec <= lt / 16 keeps |ap|_2 / |ab| below
+//    7100 and that error below 1/200, which the constants' margins cover.
+// The FP64 routine's point is within 2^-36 M of the exact projection, far
+// inside either bound.  Returns +inf where no bound applies.
+__device__ __forceinline__ float region_error(int kind, float lip, float sd, float ap, float lt, float ec)
+{
+  const float base = __fadd_ru(__fmul_ru(0.25f, lip), __fmul_ru(0x1p-23f, sd));
+  if(kind == 0) return base;
+  if(kind == 1 && __fmul_ru(ap, ec) <= 0.0625f * lt)
+    return __fadd_ru(base, __fadd_ru(__fmul_ru(0x1p-19f, ap), __fmul_ru(0x1p-20f, lt)));
+  return INFINITY;
 }
 
 // leaf_prefilter that also bounds, for the triangles it keeps, the squared
@@ -348,9 +378,10 @@ __device__ __forceinline__ int leaf_prefilter_bounds(const LeafRec32<NPC>* __res
     const float* B = v + 3 * (s + 1);
     const float* C = v + 3 * (s + 2);
     float off[3];
-    const float d2 = dist2_f32_flat(c.qf, A, B, C, off);
+    int kind;
+    const float d2 = dist2_f32_flat(c.qf, A, B, C, off, kind);
     const float ap = fmaxf(fabsf(c.qf[0] - A[0]), fmaxf(fabsf(c.qf[1] - A[1]), fabsf(c.qf[2] - A[2])));
-    const float E = __fadd_ru(c.lip, __fmul_ru(ec[s], __fadd_ru(ap, lt[s])));
+    float E = __fadd_ru(c.lip, __fmul_ru(ec[s], __fadd_ru(ap, lt[s])));
     const float lim = __fadd_ru(c.thr_leaf, E);
     if(!(d2 > __fmul_ru(__fmul_ru(lim, lim), 1.0f + 0x1p-20f)))
     {
@@ -364,12 +395,18 @@ __device__ __forceinline__ int leaf_prefilter_bounds(const LeafRec32<NPC>* __res
         const float kl = __fdiv_ru(kappa, lt[s]);
         fz = __fmul_ru(2e-12f, __fadd_ru(kl, __fdiv_ru(__fmul_ru(kl, kl), lt[s])));
       }
-      // no fuzzy displacement when every region test is clear of its EPS band
-      if(crisp_regions(c.qf, A, B, C, 0.5f * c.lip)) fz = 0.f;
       // sqrt(d2 (1 -+ 2^-20)) from the correctly rounded sqrt(d2): the factor
       // 1 -+ 2^-20 covers both the 2^-21 of the square root of the margin and
       // the 2^-24 rounding of sqrtf
       const float sd = sqrtf(d2);
+      // no fuzzy displacement when every region test is clear of its EPS band;
+      // the region is then certain, and a vertex or an edge at A has a
+      // tighter error than the general one
+      if(crisp_regions(c.qf, A, B, C, 0.5f * c.lip))
+      {
+        fz = 0.f;
+        E = fminf(E, region_error(kind, c.lip, sd, ap, lt[s], ec[s]));
+      }
       const float dl = fmaxf(__fsub_rd(__fmul_rd(sd, 1.f - 0x1p-20f), E), 0.f);
       const float dh = __fadd_ru(__fadd_ru(__fmul_ru(sd, 1.f + 0x1p-20f), E), fz);
       const float l2 = __fmul_rd(dl, dl), h2 = __fmul_ru(dh, dh);
