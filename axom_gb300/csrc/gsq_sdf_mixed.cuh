@@ -56,18 +56,22 @@ __device__ __forceinline__ float dot3f(float a0, float b0, float a1, float b1, f
 // against 0 with EPS = 1e-12) certainly has the outcome of the exact
 // comparison.  The reference's point is then the exact closest point up to
 // FP64 rounding, and its fuzzy displacement bound is not needed.
-//   u  bounds the error of every FP32 coordinate difference against the exact
-//      one: the vertices and the point are rounded to FP32 (2^-24 M, 2^-24 |q|)
-//      and the difference once more, so u = 2^-22 (|q| + M) covers all three.
-// A dot product of differences e, p is then within
-//   err_d = u (|e|_1 + |p|_1 + 6u) + 3u^2 + 2^-23 |e|_1 |p|_1
-// of the exact one (the last term: the fused dot's own rounding), a product
-// difference a b - c d within 4 D err_d + 2 err_d^2 + 2^-22 D^2 (D the largest
-// |d| plus err_d), a difference of two dots within 2 err_d + 2^-23 D.  Each
-// value must exceed twice its bound plus 2 EPS: then the FP64 value, whose own
-// rounding error is below 2^-28 of the FP32 bound, is beyond EPS with the
-// exact value's sign.
-__device__ __forceinline__ bool crisp_regions(const float* P, const float* A, const float* B, const float* C, float u)
+// Q bounds |q| per coordinate, M the mesh's coordinates.  Every dot is of an
+// edge e (ab or ac: two vertices rounded to FP32, then subtracted) and an
+// offset p (ap, bp or cp: the rounded point minus a rounded vertex).  Per
+// coordinate, e is within 2^-23 M + 2^-24 |e_d| of the exact edge and p within
+// 2^-24 (Q + M) + 2^-24 |p_d| of the exact offset (to a factor 1 + 2^-23), and
+// the fused dot rounds three times, so with E1 = max |e|_1, P1 = max |p|_1
+//   err_d = 1.02 (2^-23 M P1 + 2^-24 (Q + M) E1 + 5 2^-24 E1 P1 + 2^-44 (Q + M)^2)
+// bounds every dot's error (the last term: products of two coordinate
+// errors); a product difference a b - c d is then within 4 D err_d + 2 err_d^2
+// + 2^-22 D^2 (D the largest |d| plus err_d), a difference of two dots within
+// 2 err_d + 2^-23 D.  Each value must exceed twice its bound plus 2 EPS: then
+// the FP64 value, whose own rounding error is below 2^-28 of the FP32 bound,
+// is beyond EPS with the exact value's sign, and so is the exact value for the
+// rounded inputs (the FP32 region is the exact region for both).
+__device__ __forceinline__ bool crisp_regions(const float* P, const float* A, const float* B, const float* C, float Q,
+                                              float M)
 {
   constexpr float EPS = 1e-12f;
   const float ab0 = B[0] - A[0], ab1 = B[1] - A[1], ab2 = B[2] - A[2];
@@ -87,9 +91,11 @@ __device__ __forceinline__ bool crisp_regions(const float* P, const float* A, co
   auto n1 = [](float x, float y, float z) { return fabsf(x) + fabsf(y) + fabsf(z); };
   const float E1 = fmaxf(n1(ab0, ab1, ab2), n1(ac0, ac1, ac2));
   const float P1 = fmaxf(n1(ap0, ap1, ap2), fmaxf(n1(bp0, bp1, bp2), n1(cp0, cp1, cp2)));
-  const float err_d = __fmul_ru(1.01f, __fadd_ru(__fadd_ru(__fmul_ru(u, __fadd_ru(__fadd_ru(E1, P1), 6.f * u)),
-                                                           3.f * u * u),
-                                                  __fmul_ru(0x1p-23f, __fmul_ru(E1, P1))));
+  const float QM = __fadd_ru(Q, M);
+  const float err_d =
+      __fmul_ru(1.02f, __fadd_ru(__fadd_ru(__fmul_ru(0x1p-23f * M, P1), __fmul_ru(0x1p-24f * QM, E1)),
+                                 __fadd_ru(__fmul_ru(5.f * 0x1p-24f, __fmul_ru(E1, P1)),
+                                           __fmul_ru(0x1p-44f * QM, QM))));
   const float D = __fadd_ru(fmaxf(fmaxf(fmaxf(fabsf(d1), fabsf(d2)), fmaxf(fabsf(d3), fabsf(d4))),
                                   fmaxf(fabsf(d5), fabsf(d6))),
                             err_d);
@@ -346,9 +352,11 @@ __device__ __forceinline__ float region_error(int kind, float lip, float sd, flo
 // <= 1e-12 kappa / L, and on the products vc, vb, va (length^4), which moves
 // it by at most 1e-12 / (edge |n|) <= 1e-12 kappa^2 / L^3 (for the small
 // triangles of fine meshes this is ~1e-6, far above rounding); both doubled.
+// mesh_max bounds the mesh's coordinates (rounded up).
 template <int NPC>
 __device__ __forceinline__ int leaf_prefilter_bounds(const LeafRec32<NPC>* __restrict__ leaves32, int leafpos,
-                                                     const QCtx& c, float& lo2, float& hi2, float* cpf, float& rad)
+                                                     const QCtx& c, float mesh_max, float& lo2, float& hi2, float* cpf,
+                                                     float& rad)
 {
   const float4* r = reinterpret_cast<const float4*>(leaves32 + leafpos);
   float v[3 * NPC];
@@ -402,7 +410,8 @@ __device__ __forceinline__ int leaf_prefilter_bounds(const LeafRec32<NPC>* __res
       // no fuzzy displacement when every region test is clear of its EPS band;
       // the region is then certain, and a vertex or an edge at A has a
       // tighter error than the general one
-      if(crisp_regions(c.qf, A, B, C, 0.5f * c.lip))
+      // (the point's largest coordinate is eq 2^23 exactly)
+      if(crisp_regions(c.qf, A, B, C, c.eq * 0x1p23f, mesh_max))
       {
         fz = 0.f;
         E = fminf(E, region_error(kind, c.lip, sd, ap, lt[s], ec[s]));

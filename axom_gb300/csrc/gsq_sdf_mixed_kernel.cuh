@@ -275,7 +275,7 @@ __global__ void __launch_bounds__(128, 5) k_sdf_mixed(const NodeRec64* __restric
       {
         const int lp = -found - 1;
         float lo2, hi2, cpf[3], rad;
-        const int need = leaf_prefilter_bounds<NPC>(leaves32, lp, c, lo2, hi2, cpf, rad);
+        const int need = leaf_prefilter_bounds<NPC>(leaves32, lp, c, mesh_max, lo2, hi2, cpf, rad);
         if(AUDIT)
         {
           if(need == 0) ++st[3];
