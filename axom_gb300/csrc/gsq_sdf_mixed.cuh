@@ -163,7 +163,6 @@ struct QCtx
 {
   float qf[3];           // the point rounded to nearest
   float eq;              // bound on the point's rounding (per axis)
-  float ec;              // the same for the centroid-order test
   float lip;             // coordinate-rounding part of the triangle distance error
   float t_true, t_false; // box predicate thresholds from the interval holding minSq
   float thr_leaf;        // sqrt(upper end of that interval) + 1e-6, rounded up
@@ -177,11 +176,10 @@ __device__ __forceinline__ void qctx_init(QCtx& c, const double* q, float mesh_m
     c.qf[d] = __double2float_rn(q[d]);
     qabs = fmaxf(qabs, fabsf(c.qf[d]));
   }
-  const float Mq = fmaxf(qabs, mesh_max);
-  // |qf - q| <= 2^-24 |q|; the subtraction in a gap is exact or contributes at
-  // most 2^-24 of the gap, which the relative term of box_decide covers
-  c.eq = __fmul_ru(0x1p-23f, qabs);
-  c.ec = __fmul_ru(0x1p-18f, Mq);
+  // |qf - q| <= 2^-24 |qf| (round to nearest; the absolute term covers
+  // subnormals); the subtraction in a gap is exact or contributes at most
+  // 2^-24 of the gap, which the relative term of box_decide covers
+  c.eq = __fadd_ru(__fmul_ru(0x1p-24f, qabs), 0x1p-149f);
   // the point-triangle distance is 1-Lipschitz in the point and the vertices
   c.lip = __fmul_ru(0x1p-21f, __fadd_ru(qabs, mesh_max));
 }
@@ -231,8 +229,20 @@ __device__ __forceinline__ int box_decide(const float* lo, const float* hi, floa
 
 // One node visit decided in FP32.  Returns false if some decision is not
 // certain (the caller then decides the whole visit in FP64 with visit_fp64).
-// The child order compares 4(sl - sr) = sum_d a_d b_d with a = 2(c_L - c_R)
-// and b = 2(c_L + c_R - 2p); each factor is within dc of its exact value.
+// The child order (the nearer centroid first, LinearBVH.hpp:72-85) is the
+// sign of 4 (|c_L - q|^2 - |c_R - q|^2) = sum_d a_d b_d, built from the gaps
+// lo - q and q - hi the box tests use: per child u = (lo - q) - (q - hi) =
+// 2 (c - q), a = u_L - u_R, b = u_L + u_R.  Against the exact values of the
+// FP64 boxes and point, per axis (r the sum of the four |gaps|, s_L, s_R the
+// boxes' rounding slacks, eq the point's):
+//   |da| <= 2 (s_L + s_R) + 2^-22 r          (the point cancels in a)
+//   |db| <= 2 (s_L + s_R) + 4 eq + 2^-22 r
+// (three roundings of at most 2^-24 of a gap sum each), so the dot is within
+//   (c0 + 4 eq) A1 + c0 B1 + 2^-22 sum r (|a| + |b|) + 2^-21 sum |a b|
+//   + 6 (c0 + 4 eq)^2 + 2^-43 sum r^2,      c0 = 2 (s_L + s_R),
+// A1 = sum |a|, B1 = sum |b| (the fused dot rounds three times).  The FP64
+// comparison of the rounded centroids' squared distances is within
+// 2^-50 Mq sum r (Mq the largest coordinate, below 2^21 lip) of the exact one.
 __device__ __forceinline__ bool visit32(const NodeRec32* __restrict__ nodes32, int cur, const QCtx& c, bool& inL,
                                         bool& inR, bool& swap, int2& ch)
 {
@@ -251,19 +261,27 @@ __device__ __forceinline__ bool visit32(const NodeRec32* __restrict__ nodes32, i
   swap = false;
   if(dl == 1 && dr == 1)
   {
-    float dot = 0.f, mag = 0.f, prod = 0.f;
+    float dot = 0.f, A1 = 0.f, B1 = 0.f, es = 0.f, rr = 0.f, R1 = 0.f, prod = 0.f;
 #pragma unroll
     for(int d = 0; d < 3; ++d)
     {
-      const float sL = lo_l[d] + hi_l[d], sR = lo_r[d] + hi_r[d];
-      const float av = sL - sR;
-      const float bv = (sL + sR) - 4.f * c.qf[d];
+      const float gll = lo_l[d] - c.qf[d], ghl = c.qf[d] - hi_l[d];
+      const float glr = lo_r[d] - c.qf[d], ghr = c.qf[d] - hi_r[d];
+      const float uL = gll - ghl, uR = glr - ghr;
+      const float av = uL - uR, bv = uL + uR;
       dot = __fmaf_rn(av, bv, dot);
-      mag += fabsf(av) + fabsf(bv);
-      prod += fabsf(av * bv);
+      const float aa = fabsf(av), bb = fabsf(bv);
+      const float r = (fabsf(gll) + fabsf(ghl)) + (fabsf(glr) + fabsf(ghr));
+      A1 += aa;
+      B1 += bb;
+      R1 += r;
+      es = __fmaf_rn(r, aa + bb, es);
+      rr = __fmaf_rn(r, r, rr);
+      prod = __fmaf_rn(aa, bb, prod);
     }
-    const float dc = 2.f * (sl_ + sr_) + c.ec;
-    const float bound = 1.01f * (dc * mag + 3.f * dc * dc + 0x1p-20f * prod);
+    const float c0 = 2.f * (sl_ + sr_), c04 = c0 + 4.f * c.eq;
+    const float bound = 1.02f * (c04 * A1 + c0 * B1 + 0x1p-22f * es + 0x1p-21f * prod + 6.f * c04 * c04 +
+                                 0x1p-43f * rr + 0x1p-29f * c.lip * R1);
     if(!(bound < INFINITY)) return false;
     if(dot > bound)
       swap = true;
@@ -410,8 +428,8 @@ __device__ __forceinline__ int leaf_prefilter_bounds(const LeafRec32<NPC>* __res
       // no fuzzy displacement when every region test is clear of its EPS band;
       // the region is then certain, and a vertex or an edge at A has a
       // tighter error than the general one
-      // (the point's largest coordinate is eq 2^23 exactly)
-      if(crisp_regions(c.qf, A, B, C, c.eq * 0x1p23f, mesh_max))
+      // (eq 2^24 bounds the point's largest coordinate)
+      if(crisp_regions(c.qf, A, B, C, c.eq * 0x1p24f, mesh_max))
       {
         fz = 0.f;
         E = fminf(E, region_error(kind, c.lip, sd, ap, lt[s], ec[s]));
@@ -491,7 +509,16 @@ __device__ __forceinline__ bool mixed_traverse(const double* q, MinCand& mc, con
   qctx_init(c, q, mesh_max);
   qctx_update(c, mc.minSq);
   auto visit = [&](int cur, bool& inL, bool& inR, bool& swap, int2& ch) {
-    if(visit32(nodes32, cur, c, inL, inR, swap, ch)) return;
+    if(visit32(nodes32, cur, c, inL, inR, swap, ch))
+    {
+      if(AUDIT)
+      {
+        bool a2, b2, w2;
+        visit_fp64(nodes64, cur, q, mc.minSq, a2, b2, w2);
+        if(a2 != inL || b2 != inR || (inL && inR && w2 != swap)) ++stats[0];
+      }
+      return;
+    }
     if(AUDIT) ++stats[1];
     visit_fp64(nodes64, cur, q, mc.minSq, inL, inR, swap);
   };

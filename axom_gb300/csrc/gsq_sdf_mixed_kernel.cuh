@@ -370,7 +370,20 @@ __global__ void __launch_bounds__(128, 5) k_sdf_mixed(const NodeRec64* __restric
       bool inL, inR, swap;
       int2 ch;
       if(visit32(nodes32, cur, c, inL, inR, swap, ch))
+      {
+        if(AUDIT)
+        {
+          // the FP64 visit at the exact minimum (the queue refined on a copy)
+          // must take the same decisions
+          MinCand s1 = mc;
+          if(reset) init_min(s1);
+          for(int j = 0; j < np; ++j) leaf_refine<NPC>(leaves64, pq[j] >> 2, pq[j] & 3, q, s1, computeNormal);
+          bool a2, b2, w2;
+          visit_fp64(nodes64, cur, q, s1.minSq, a2, b2, w2);
+          if(a2 != inL || b2 != inR || (inL && inR && w2 != swap)) ++st[0];
+        }
         apply_visit(inL, inR, swap, ch);
+      }
       else
       {
         pend = P_NODE;
