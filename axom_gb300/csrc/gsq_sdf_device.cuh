@@ -307,11 +307,15 @@ __device__ __forceinline__ void init_min(MinCand& mc)
   mc.npend = 0;
 }
 
-// Sign (SD:583-592) and outputs (SD:594-603) of one query.
-template <int NPC>
+// Sign (SD:583-592) and outputs (SD:594-603) of one query.  sign_hint() may
+// return the certain outcome of the sign test (+1 or -1; 0 when unknown); it
+// is asked only when the sign is needed and no normal is written, and then
+// saves the FP64 pseudo-normal.
+template <int NPC, class SignHint>
 __device__ __forceinline__ void finish_query(const double* q, const MinCand& mc, const LeafRec<NPC>* __restrict__ leaves,
                                              const SdfParams& prm, int idx, double* __restrict__ out,
-                                             double* __restrict__ out_cp, double* __restrict__ out_n)
+                                             double* __restrict__ out_cp, double* __restrict__ out_n,
+                                             SignHint sign_hint)
 {
   // getSurfaceNormal (SD:740-748); the recorded pseudo-normal terms are
   // evaluated only when the normal is used
@@ -320,7 +324,8 @@ __device__ __forceinline__ void finish_query(const double* q, const MinCand& mc,
   const bool inside_box = !(mc.mp[0] < D[0] || mc.mp[0] > D[3] || mc.mp[1] < D[1] || mc.mp[1] > D[4] ||
                             mc.mp[2] < D[2] || mc.mp[2] > D[5]);
   const bool want_sign = prm.sign && !(prm.watertight && !inside_box);
-  if(mc.type == 2)
+  const double hint = (want_sign && !out_n) ? sign_hint() : 0.0;
+  if(hint == 0.0 && mc.type == 2)
   {
     double v[3 * NPC];
     load_leaf<NPC>(leaves, mc.leaf, v);
@@ -329,14 +334,16 @@ __device__ __forceinline__ void finish_query(const double* q, const MinCand& mc,
     else
       tri_normal(v, v + 3, v + 6, nrm);
   }
-  else if(mc.npend > 0 && (want_sign || out_n))
+  else if(hint == 0.0 && mc.npend > 0 && (want_sign || out_n))
   {
     MinCand m = mc;
     flush_normals<NPC>(m, leaves);
     nrm[0] = m.sn[0], nrm[1] = m.sn[1], nrm[2] = m.sn[2];
   }
   double sgn = 1.0;
-  if(want_sign)
+  if(hint != 0.0)
+    sgn = hint;
+  else if(want_sign)
   {
     // computeSign (SD:751-763)
     const double r0 = q[0] - mc.mp[0], r1 = q[1] - mc.mp[1], r2 = q[2] - mc.mp[2];
@@ -357,6 +364,39 @@ __device__ __forceinline__ void finish_query(const double* q, const MinCand& mc,
     out_n[3 * (size_t)idx + 1] = u[1];
     out_n[3 * (size_t)idx + 2] = u[2];
   }
+}
+
+template <int NPC>
+__device__ __forceinline__ void finish_query(const double* q, const MinCand& mc, const LeafRec<NPC>* __restrict__ leaves,
+                                             const SdfParams& prm, int idx, double* __restrict__ out,
+                                             double* __restrict__ out_cp, double* __restrict__ out_n)
+{
+  finish_query<NPC>(q, mc, leaves, prm, idx, out, out_cp, out_n, [] { return 0.0; });
+}
+
+// computeSign's outcome (SD:751-763) in FP64, as finish_query forms it when the
+// sign is needed (used to audit certified signs).
+template <int NPC>
+__device__ __forceinline__ double sign64(const double* q, const MinCand& mc, const LeafRec<NPC>* __restrict__ leaves)
+{
+  double nrm[3] = {mc.sn[0], mc.sn[1], mc.sn[2]};
+  if(mc.type == 2)
+  {
+    double v[3 * NPC];
+    load_leaf<NPC>(leaves, mc.leaf, v);
+    if(NPC == 4 && mc.sub == 1)
+      tri_normal(v, v + 6, v + 9, nrm);
+    else
+      tri_normal(v, v + 3, v + 6, nrm);
+  }
+  else if(mc.npend > 0)
+  {
+    MinCand m = mc;
+    flush_normals<NPC>(m, leaves);
+    nrm[0] = m.sn[0], nrm[1] = m.sn[1], nrm[2] = m.sn[2];
+  }
+  const double r0 = q[0] - mc.mp[0], r1 = q[1] - mc.mp[1], r2 = q[2] - mc.mp[2];
+  return (dot3(r0, r1, r2, nrm[0], nrm[1], nrm[2]) >= 0.0) ? 1.0 : -1.0;
 }
 
 // Leaf action of the reference (the searchMinDist lambda, SD:570-574) on one

@@ -252,15 +252,22 @@ __global__ void __launch_bounds__(128, 5) k_sdf_mixed(const NodeRec64* __restric
       }
       else if(p == P_FINISH)
       {
+        // the sign certified in FP32 where possible (the FP64 pseudo-normal
+        // is then not formed); the audit checks it against FP64
+        auto hint = [&] {
+          const double h = sign32<NPC>(q, mc, leaves32, mesh_max);
+          if(AUDIT && h != 0.0 && h != sign64<NPC>(q, mc, leaves64)) ++st[0];
+          return h;
+        };
         if constexpr(MULTI)
         {
           SdfParams prm = prm_all;
           const MeshInfo& mi = meshes[mesh_of(idx)];
           for(int d = 0; d < 6; ++d) prm.domain[d] = mi.domain[d];
-          finish_query<NPC>(q, mc, leaves64, prm, idx, out, out_cp, out_n);
+          finish_query<NPC>(q, mc, leaves64, prm, idx, out, out_cp, out_n, hint);
         }
         else
-          finish_query<NPC>(q, mc, leaves64, prm_all, idx, out, out_cp, out_n);
+          finish_query<NPC>(q, mc, leaves64, prm_all, idx, out, out_cp, out_n, hint);
         mode = M_IDLE;
       }
       continue;

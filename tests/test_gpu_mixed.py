@@ -78,6 +78,11 @@ def test_mixed_equals_fp64_with_audit(gsq, case):
     assert_bits_equal(cpm, cp64, "closest point")
     np.testing.assert_allclose(nm, n64, rtol=0, atol=1e-12)
     assert st["leaf_skipped"] > 0
+    # without normals the sign is certified in FP32 where it can be; the audit
+    # checks every certified sign against the FP64 pseudo-normal test
+    dm2 = sd.compute_distances(q)
+    assert sd.mixed_stats()["violations"] == 0
+    assert_bits_equal(dm2, d64, "distance, FP32-certified signs (audited)")
     sd.set_audit(False)
     assert_bits_equal(sd.compute_distances(q), d64, "distance without audit")
 
