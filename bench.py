@@ -41,8 +41,8 @@ FALLBACK_HBM_GBS = 6800.0
 BATCH_MESHES = 512
 # DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) per point of one
 # k_sdf_mixed launch, measured by ncu on 1,048,576 uniform points of the same
-# mesh (3.083 GB read + 1.237 GB written); the bench scales it by its point count.
-MIXED_DRAM_BYTES_PER_POINT = (3.083479e9 + 1.237160e9) / 1048576
+# mesh (1.432 GB read + 0.373 GB written); the bench scales it by its point count.
+MIXED_DRAM_BYTES_PER_POINT = (1.432073e9 + 0.373072e9) / 1048576
 BATCH_SEED = 5
 
 
