@@ -27,8 +27,8 @@ struct MixedStats
 // minimum and certified bounds of the queued candidates' FP64 distances), and
 // every later decision is certified against the whole interval.  A lane parks
 // when its queue is full, when a node decision is uncertain, or at its end;
-// once every live lane of the warp is parked (or BATCH_MIN are) the warp
-// replays the parked lanes' queues in order in FP64, converged.  The FP64 state
+// once every live lane of the warp is parked (or enough are, see below) the
+// warp replays the parked lanes' queues in order in FP64, converged.  The FP64 state
 // therefore evolves through exactly the reference's checkCandidate calls on
 // exactly the reference's candidates.  Finished lanes take the next point from
 // the queue of Morton-ordered points with one warp-aggregated atomic.
@@ -37,7 +37,15 @@ struct MixedStats
 // tree is shallow enough).  MULTI: the points belong to several meshes (point
 // ranges qoff[k].. of mesh k, whose records start at meshes[k]'s offsets);
 // otherwise to the one mesh meshes[0] with its node box in prm_all.
-constexpr int BATCH_MIN = 16;
+//
+// Batch size: a batch costs about the same whatever its lanes, and a parked
+// lane idles until the batch, so with parks arriving at rate lam per iteration
+// the cost per park C / N + N / (2 lam) is least at N ~ sqrt(2 C lam).  Each
+// warp tracks lam (a moving average of parked lanes per iteration between
+// batches) and fires at N = 38.5 sqrt(lam) parked lanes, clamped to 8..24 (the
+// constant measured: about 12 for uniform points, 24 near the surface).
+constexpr float BATCH_K = 38.5f, BATCH_LAM0 = 0.1f;
+constexpr int BATCH_LO = 8, BATCH_HI = 24;
 
 template <int NPC, bool AUDIT, int QCAP, int STK, bool MULTI>
 __global__ void __launch_bounds__(128, 5) k_sdf_mixed(const NodeRec64* __restrict__ nodes64_all,
@@ -105,6 +113,8 @@ __global__ void __launch_bounds__(128, 5) k_sdf_mixed(const NodeRec64* __restric
   int mode = M_IDLE, pend = P_NONE;
   int2 pch = make_int2(0, 0);
   bool open = true;
+  float lam = BATCH_LAM0;  // parks per iteration (warp-uniform moving average)
+  int bmin = 12, since = 0;
   unsigned long long st[4] = {0, 0, 0, 0};
 
   auto set_thresholds = [&]() {
@@ -210,8 +220,12 @@ __global__ void __launch_bounds__(128, 5) k_sdf_mixed(const NodeRec64* __restric
     const unsigned live = __ballot_sync(FULL, mode != M_IDLE);
     if(live == 0) break;
     const unsigned parked = __ballot_sync(FULL, pend != P_NONE);
-    if(parked && (parked == live || __popc(parked) >= BATCH_MIN))
+    ++since;
+    if(parked && (parked == live || __popc(parked) >= bmin))
     {
+      lam = 0.875f * lam + 0.125f * (float)__popc(parked) / (float)since;
+      bmin = (int)fminf(fmaxf(BATCH_K * sqrtf(lam), (float)BATCH_LO), (float)BATCH_HI);
+      since = 0;
       // converged FP64 work of the parked lanes: replay the queue in order
       const int p = pend;
       pend = P_NONE;
