@@ -89,6 +89,17 @@ __device__ __forceinline__ void tri_error_terms(const double* A, const double* B
                              sqrt(bc[0] * bc[0] + bc[1] * bc[1] + bc[2] * bc[2])));
   const double kappa = (nn > 0.0 && nn == nn) ? (L * L) / nn : INFINITY;
   ec = __double2float_ru(256.0 * 0x1p-24 * kappa * 1.01);
+  // The reference's fuzzy dot tests (EPS = 1e-12 on d1..d6) can leave its
+  // point up to EPS / (shortest edge) <= 1e-12 kappa / L off the triangle (an
+  // edge parameter d1 / (d1 - d3) with d1 in [-EPS, 0)), nearer the query than
+  // the exact distance.  The coordinate term lip of the FP32 error bound holds
+  // 0.78 lip >= 2^-22 M of slack beyond the rounding it covers; where the
+  // overshoot could exceed 2^-22 times the triangle's largest coordinate (tiny
+  // triangles), the conditioning factor is made infinite, so that the
+  // triangle is never skipped and its bounds come from FP64.
+  const double mt = fmax(fmax(fmax(fabs(A[0]), fabs(A[1])), fmax(fabs(A[2]), fabs(B[0]))),
+                         fmax(fmax(fabs(B[1]), fabs(B[2])), fmax(fmax(fabs(C[0]), fabs(C[1])), fabs(C[2]))));
+  if(!(2.06e-12 * kappa / L <= 0x1p-22 * mt)) ec = INFINITY;
   lt = __double2float_ru(L * 1.0001);
   if(fz)
   {
