@@ -3,6 +3,7 @@
 #pragma once
 
 #include "gsq_sdf_device.cuh"
+#include "gsq_sign.cuh"
 
 namespace gsq
 {
@@ -448,32 +449,47 @@ __device__ __forceinline__ int leaf_prefilter_bounds(const LeafRec32<NPC>* __res
   return need;
 }
 
-// FP32 certificate of computeSign (SD:751-763): +1 or -1 when the FP64
-// dot(q - cp, N) >= 0 of finish_query certainly has that outcome, 0 when not
-// certain (the caller then evaluates the pseudo-normal in FP64).  N is the
-// face normal (type 2) or the pseudo-normal sum: sn plus the recorded
-// contributions, each rebuilt here in FP32 from the rounded vertices.
-// Error terms (u = 2^-24, M the mesh bound, L the triangle's longest edge):
-//  * an edge of rounded vertices is within de = 2^-23 M + u L per coordinate;
-//  * a cross product of two edges within dn = 3 (4 de L + 2 de^2 + 2^-22 L^2)
-//    in L1 (two products and a fused subtraction per coordinate);
-//  * a normalised vector v within 2 |dv| / (|v| - |dv|) + 4u (direction of a
-//    perturbed vector, then the correctly rounded 1/sqrt and the scaling);
-//  * the angle acos(ua . ub) within w(ddp) + 2^-21: ddp bounds the dot's
-//    error, w(t) = t / sqrt(1 - (|x| + t)^2) away from +-1 and pi sqrt(t / 2)
-//    everywhere (acos's modulus of continuity), 2^-21 the 2 ulp of acosf;
-//  * FP32 sums round at most u per term and addition;
-//  * r = q - cp is formed in FP64 as the reference forms it and rounded (u).
-// The FP64 evaluation's own rounding is below 2^-40 of these bounds.
+// The roundings the sign certificate asks for, as device intrinsics (the
+// certificate is evaluated on the device; the host checker supplies its own).
+struct SignOps
+{
+#ifdef __CUDA_ARCH__
+  __host__ __device__ static float fma(float a, float b, float c) { return __fmaf_rn(a, b, c); }
+  __host__ __device__ static float add_ru(float a, float b) { return __fadd_ru(a, b); }
+  __host__ __device__ static float add_rd(float a, float b) { return __fadd_rd(a, b); }
+  __host__ __device__ static float sub_rd(float a, float b) { return __fsub_rd(a, b); }
+  __host__ __device__ static float mul_ru(float a, float b) { return __fmul_ru(a, b); }
+  __host__ __device__ static float mul_rd(float a, float b) { return __fmul_rd(a, b); }
+  __host__ __device__ static float div_ru(float a, float b) { return __fdiv_ru(a, b); }
+  __host__ __device__ static float rsqrt(float a) { return __frsqrt_rn(a); }
+  __host__ __device__ static float acos(float a) { return acosf(a); }
+  __host__ __device__ static float to_float(double a) { return __double2float_rn(a); }
+#else
+  static float fma(float a, float b, float c) { return fmaf(a, b, c); }
+  static float add_ru(float a, float b) { return nextafterf(a + b, INFINITY); }
+  static float add_rd(float a, float b) { return nextafterf(a + b, -INFINITY); }
+  static float sub_rd(float a, float b) { return nextafterf(a - b, -INFINITY); }
+  static float mul_ru(float a, float b) { return nextafterf(a * b, INFINITY); }
+  static float mul_rd(float a, float b) { return nextafterf(a * b, -INFINITY); }
+  static float div_ru(float a, float b) { return nextafterf(a / b, INFINITY); }
+  static float rsqrt(float a) { return (float)(1.0 / sqrt((double)a)); }
+  static float acos(float a) { return (float)::acos((double)a); }
+  static float to_float(double a) { return (float)a; }
+#endif
+};
+
+// FP32 certificate of computeSign (SD:751-763) for one finished query (see
+// gsq_sign.cuh): +1 or -1 when the FP64 dot(q - cp, N) >= 0 of finish_query
+// certainly has that outcome, 0 when not certain (the caller then evaluates
+// the pseudo-normal in FP64).  The triangles come from the FP32 leaf records:
+// the closest face (type 2) or the recorded pseudo-normal contributions.
 template <int NPC>
 __device__ __forceinline__ double sign32(const double* q, const MinCand& mc, const LeafRec32<NPC>* __restrict__ leaves32,
                                          float M)
 {
-  constexpr float U = 0x1p-24f;
   const float r[3] = {__double2float_rn(q[0] - mc.mp[0]), __double2float_rn(q[1] - mc.mp[1]),
                       __double2float_rn(q[2] - mc.mp[2])};
-  // the triangle's vertices in FP32 and its longest edge
-  auto tri = [&](int leaf, int sub, const float*& A, const float*& B, const float*& C, float& L) {
+  auto rec_tri = [&](int leaf, int sub, const float*& A, const float*& B, const float*& C, float& L) {
     const LeafRec32<NPC>& rec = leaves32[leaf];
     A = rec.v;
     B = rec.v + 3 * (sub + 1);
@@ -483,106 +499,20 @@ __device__ __forceinline__ double sign32(const double* q, const MinCand& mc, con
     else
       L = rec.lt[sub];
   };
-  // cross(B - A, C - A) and the L1 bound on its error
-  auto normal = [&](const float* A, const float* B, const float* C, float L, float* n) {
-    const float e1[3] = {B[0] - A[0], B[1] - A[1], B[2] - A[2]};
-    const float e2[3] = {C[0] - A[0], C[1] - A[1], C[2] - A[2]};
-    n[0] = __fmaf_rn(e1[1], e2[2], -(e2[1] * e1[2]));
-    n[1] = __fmaf_rn(e2[0], e1[2], -(e1[0] * e2[2]));
-    n[2] = __fmaf_rn(e1[0], e2[1], -(e2[0] * e1[1]));
-    const float de = __fadd_ru(0x1p-23f * M, __fmul_ru(U, L));
-    return __fmul_ru(3.f, __fadd_ru(__fadd_ru(__fmul_ru(4.f * de, L), __fmul_ru(2.f * de, de)),
-                                    __fmul_ru(0x1p-22f, __fmul_ru(L, L))));
-  };
-  // v / |v| and the L2 bound on its error given |dv|_2 <= dv; false if v is
-  // too short to bound
-  auto unit = [&](const float* v, float dv, float* o, float& du) {
-    const float l2 = dot3f(v[0], v[0], v[1], v[1], v[2], v[2]);
-    const float len = sqrtf(l2);
-    const float gap = __fsub_rd(__fmul_rd(len, 1.f - 0x1p-21f), dv);
-    if(!(gap > 0x1p-100f) || !(gap > dv)) return false;
-    const float s = __frsqrt_rn(l2);
-    o[0] = v[0] * s, o[1] = v[1] * s, o[2] = v[2] * s;
-    du = __fadd_ru(__fdiv_ru(2.f * dv, gap), 4.f * U);
-    return true;
-  };
-  float n[3], en;
   if(mc.type == 2)
   {
-    const float *A, *B, *C;
-    float L;
-    tri(mc.leaf, mc.sub, A, B, C, L);
-    en = normal(A, B, C, L, n);
+    auto face_tri = [&](int, const float*& A, const float*& B, const float*& C, float& L, int& k) {
+      k = 0;
+      rec_tri(mc.leaf, mc.sub, A, B, C, L);
+    };
+    return sign_certificate<SignOps>(r, true, mc.sn, 1, face_tri, M);
   }
-  else
-  {
-    n[0] = __double2float_rn(mc.sn[0]), n[1] = __double2float_rn(mc.sn[1]), n[2] = __double2float_rn(mc.sn[2]);
-    float mag = fabsf(n[0]) + fabsf(n[1]) + fabsf(n[2]);
-    en = __fmul_ru(U, mag);
-    for(int i = 0; i < mc.npend; ++i)
-    {
-      const int code = mc.pend[i];
-      const float *A, *B, *C;
-      float L;
-      tri(code >> 3, (code >> 2) & 1, A, B, C, L);
-      const int k = code & 3;
-      float nt[3], u[3], du;
-      const float dn = normal(A, B, C, L, nt);
-      if(k != 3)
-      {
-        // degenerate (Triangle.hpp:327-330): area = |n| / 2 <= 1e-12
-        const float len = sqrtf(dot3f(nt[0], nt[0], nt[1], nt[1], nt[2], nt[2]));
-        const float lo = __fmul_rd(__fsub_rd(len, dn), 0.5f - 0x1p-22f);
-        const float hi = __fmul_ru(__fadd_ru(len, dn), 0.5f + 0x1p-22f);
-        if(hi < 0.999e-12f) continue;  // certainly degenerate: no contribution
-        if(!(lo > 1.001e-12f)) return 0.0;
-      }
-      if(!unit(nt, dn, u, du)) return 0.0;
-      float c[3], ec;
-      if(k == 3)
-      {
-        c[0] = u[0], c[1] = u[1], c[2] = u[2];
-        ec = __fmul_ru(1.7321f, du);
-      }
-      else
-      {
-        // Triangle::angle (Triangle.hpp:385-400) at vertex k
-        const float* V[3] = {A, B, C};
-        const float* pt = V[k];
-        const float* p1 = V[(k + 1) % 3];
-        const float* p2 = V[(k + 2) % 3];
-        const float a[3] = {p1[0] - pt[0], p1[1] - pt[1], p1[2] - pt[2]};
-        const float b[3] = {p2[0] - pt[0], p2[1] - pt[1], p2[2] - pt[2]};
-        const float de = __fmul_ru(1.7321f, __fadd_ru(0x1p-23f * M, __fmul_ru(U, L)));
-        float ua[3], ub[3], dua, dub;
-        if(!unit(a, de, ua, dua) || !unit(b, de, ub, dub)) return 0.0;
-        const float dp = fminf(fmaxf(dot3f(ua[0], ub[0], ua[1], ub[1], ua[2], ub[2]), -1.f), 1.f);
-        const float ddp = __fadd_ru(__fadd_ru(dua, dub), __fadd_ru(__fmul_ru(dua, dub), 4.f * U));
-        float dal = __fmul_ru(3.1416f, sqrtf(__fmul_ru(0.5f, ddp)) * (1.f + 0x1p-20f));
-        const float x = __fadd_ru(fabsf(dp), ddp);
-        if(x < 1.f)
-          dal = fminf(dal, __fdiv_ru(ddp, __fmul_rd(sqrtf(__fmul_rd(__fsub_rd(1.f, x), __fadd_rd(1.f, x))),
-                                                    1.f - 0x1p-20f)));
-        dal = __fadd_ru(dal, 0x1p-21f);
-        const float al = acosf(dp);
-        c[0] = u[0] * al, c[1] = u[1] * al, c[2] = u[2] * al;
-        // |d(al u)|_1 <= sqrt(3) (dal + (al + dal) du) plus the products' rounding
-        ec = __fmul_ru(1.7321f, __fadd_ru(__fadd_ru(dal, __fmul_ru(__fadd_ru(al, dal), du)), __fmul_ru(U, al)));
-      }
-      n[0] += c[0], n[1] += c[1], n[2] += c[2];
-      mag = __fadd_ru(mag, fabsf(c[0]) + fabsf(c[1]) + fabsf(c[2]));
-      // this term's error and the rounding of the running sum
-      en = __fadd_ru(en, __fadd_ru(ec, __fmul_ru(2.f * U, mag)));
-    }
-  }
-  const float s = dot3f(r[0], n[0], r[1], n[1], r[2], n[2]);
-  const float rmax = fmaxf(fabsf(r[0]), fmaxf(fabsf(r[1]), fabsf(r[2])));
-  const float rn = __fadd_ru(__fadd_ru(fabsf(r[0] * n[0]), fabsf(r[1] * n[1])), fabsf(r[2] * n[2]));
-  const float err = __fmul_ru(1.05f, __fadd_ru(__fmul_ru(rmax, en), __fmul_ru(5.f * U, rn)));
-  if(!(err < INFINITY)) return 0.0;
-  if(s > err) return 1.0;
-  if(s < -err) return -1.0;
-  return 0.0;
+  auto pend_tri = [&](int i, const float*& A, const float*& B, const float*& C, float& L, int& k) {
+    const int code = mc.pend[i];
+    k = code & 3;
+    rec_tri(code >> 3, (code >> 2) & 1, A, B, C, L);
+  };
+  return sign_certificate<SignOps>(r, false, mc.sn, mc.npend, pend_tri, M);
 }
 
 // Audit of a skipped triangle: counts it if the FP64 distance contradicts
