@@ -72,43 +72,6 @@ __global__ void k_nodes32(const NodeRec64* __restrict__ in, int n_inner, NodeRec
   out[i] = r;
 }
 
-// Per triangle: ec = 256 * 2^-24 * kappa (kappa = L^2 / |n|, L the longest
-// edge), lt = L, and fz = 2e-12 (kappa / L + kappa^2 / L^3), the bound on how
-// far the reference's fuzzy region tests move its closest point; all rounded
-// up with a margin.
-__device__ __forceinline__ void tri_error_terms(const double* A, const double* B, const double* C, float& ec, float& lt,
-                                                float* fz = nullptr)
-{
-  const double ab[3] = {B[0] - A[0], B[1] - A[1], B[2] - A[2]};
-  const double ac[3] = {C[0] - A[0], C[1] - A[1], C[2] - A[2]};
-  const double bc[3] = {C[0] - B[0], C[1] - B[1], C[2] - B[2]};
-  const double n[3] = {ab[1] * ac[2] - ab[2] * ac[1], ab[2] * ac[0] - ab[0] * ac[2], ab[0] * ac[1] - ab[1] * ac[0]};
-  const double nn = sqrt(n[0] * n[0] + n[1] * n[1] + n[2] * n[2]);
-  const double L = fmax(sqrt(ab[0] * ab[0] + ab[1] * ab[1] + ab[2] * ab[2]),
-                        fmax(sqrt(ac[0] * ac[0] + ac[1] * ac[1] + ac[2] * ac[2]),
-                             sqrt(bc[0] * bc[0] + bc[1] * bc[1] + bc[2] * bc[2])));
-  const double kappa = (nn > 0.0 && nn == nn) ? (L * L) / nn : INFINITY;
-  ec = __double2float_ru(256.0 * 0x1p-24 * kappa * 1.01);
-  // The reference's fuzzy dot tests (EPS = 1e-12 on d1..d6) can leave its
-  // point up to EPS / (shortest edge) <= 1e-12 kappa / L off the triangle (an
-  // edge parameter d1 / (d1 - d3) with d1 in [-EPS, 0)), nearer the query than
-  // the exact distance.  The coordinate term lip of the FP32 error bound holds
-  // 0.78 lip >= 2^-22 M of slack beyond the rounding it covers; where the
-  // overshoot could exceed 2^-22 times the triangle's largest coordinate (tiny
-  // triangles), the conditioning factor is made infinite, so that the
-  // triangle is never skipped and its bounds come from FP64.
-  const double mt = fmax(fmax(fmax(fabs(A[0]), fabs(A[1])), fmax(fabs(A[2]), fabs(B[0]))),
-                         fmax(fmax(fabs(B[1]), fabs(B[2])), fmax(fmax(fabs(C[0]), fabs(C[1])), fabs(C[2]))));
-  if(!(2.06e-12 * kappa / L <= 0x1p-22 * mt)) ec = INFINITY;
-  lt = __double2float_ru(L * 1.0001);
-  if(fz)
-  {
-    const double kl = kappa / L;
-    const double f = 2e-12 * (kl + kl * kappa / (L * L)) * 1.03;
-    *fz = (f == f) ? __double2float_ru(f) : INFINITY;
-  }
-}
-
 template <int NPC>
 __global__ void k_leaves32(const LeafRec<NPC>* __restrict__ in, int n, LeafRec32<NPC>* __restrict__ out)
 {

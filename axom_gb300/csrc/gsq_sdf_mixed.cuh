@@ -2,6 +2,7 @@
 // distance, shared by the mixed query kernel and the adjoint kernel.
 #pragma once
 
+#include "gsq_leaf32.cuh"
 #include "gsq_sdf_device.cuh"
 #include "gsq_sign.cuh"
 
@@ -44,164 +45,6 @@ struct MeshInfo
 
 namespace sdf
 {
-// FP32 dot product with fused operations (one rounding per multiply-add):
-// the error bounds used with these FP32 evaluations count at least one
-// rounding per operation, which fused operations meet.
-__device__ __forceinline__ float dot3f(float a0, float b0, float a1, float b1, float a2, float b2)
-{
-  return __fmaf_rn(a2, b2, __fmaf_rn(a1, b1, a0 * b0));
-}
-
-// True when every fuzzy comparison of the reference's closest_point
-// (closest_point.hpp:181-282: d1..d6, d4 - d3, d5 - d6, d1 - d3 and vc, vb, va
-// against 0 with EPS = 1e-12) certainly has the outcome of the exact
-// comparison.  The reference's point is then the exact closest point up to
-// FP64 rounding, and its fuzzy displacement bound is not needed.
-// Q bounds |q| per coordinate, M the mesh's coordinates.  Every dot is of an
-// edge e (ab or ac: two vertices rounded to FP32, then subtracted) and an
-// offset p (ap, bp or cp: the rounded point minus a rounded vertex).  Per
-// coordinate, e is within 2^-23 M + 2^-24 |e_d| of the exact edge and p within
-// 2^-24 (Q + M) + 2^-24 |p_d| of the exact offset (to a factor 1 + 2^-23), and
-// the fused dot rounds three times, so with E1 = max |e|_1, P1 = max |p|_1
-//   err_d = 1.02 (2^-23 M P1 + 2^-24 (Q + M) E1 + 5 2^-24 E1 P1 + 2^-44 (Q + M)^2)
-// bounds every dot's error (the last term: products of two coordinate
-// errors); a product difference a b - c d is then within 4 D err_d + 2 err_d^2
-// + 2^-22 D^2 (D the largest |d| plus err_d), a difference of two dots within
-// 2 err_d + 2^-23 D.  Each value must exceed twice its bound plus 2 EPS: then
-// the FP64 value, whose own rounding error is below 2^-28 of the FP32 bound,
-// is beyond EPS with the exact value's sign, and so is the exact value for the
-// rounded inputs (the FP32 region is the exact region for both).
-__device__ __forceinline__ bool crisp_regions(const float* P, const float* A, const float* B, const float* C, float Q,
-                                              float M)
-{
-  constexpr float EPS = 1e-12f;
-  const float ab0 = B[0] - A[0], ab1 = B[1] - A[1], ab2 = B[2] - A[2];
-  const float ac0 = C[0] - A[0], ac1 = C[1] - A[1], ac2 = C[2] - A[2];
-  const float ap0 = P[0] - A[0], ap1 = P[1] - A[1], ap2 = P[2] - A[2];
-  const float bp0 = P[0] - B[0], bp1 = P[1] - B[1], bp2 = P[2] - B[2];
-  const float cp0 = P[0] - C[0], cp1 = P[1] - C[1], cp2 = P[2] - C[2];
-  const float d1 = dot3f(ab0, ap0, ab1, ap1, ab2, ap2);
-  const float d2 = dot3f(ac0, ap0, ac1, ap1, ac2, ap2);
-  const float d3 = dot3f(ab0, bp0, ab1, bp1, ab2, bp2);
-  const float d4 = dot3f(ac0, bp0, ac1, bp1, ac2, bp2);
-  const float d5 = dot3f(ab0, cp0, ab1, cp1, ab2, cp2);
-  const float d6 = dot3f(ac0, cp0, ac1, cp1, ac2, cp2);
-  const float vc = __fmaf_rn(d1, d4, -(d3 * d2));
-  const float vb = __fmaf_rn(d5, d2, -(d1 * d6));
-  const float va = __fmaf_rn(d3, d6, -(d5 * d4));
-  auto n1 = [](float x, float y, float z) { return fabsf(x) + fabsf(y) + fabsf(z); };
-  const float E1 = fmaxf(n1(ab0, ab1, ab2), n1(ac0, ac1, ac2));
-  const float P1 = fmaxf(n1(ap0, ap1, ap2), fmaxf(n1(bp0, bp1, bp2), n1(cp0, cp1, cp2)));
-  const float QM = __fadd_ru(Q, M);
-  const float err_d =
-      __fmul_ru(1.02f, __fadd_ru(__fadd_ru(__fmul_ru(0x1p-23f * M, P1), __fmul_ru(0x1p-24f * QM, E1)),
-                                 __fadd_ru(__fmul_ru(5.f * 0x1p-24f, __fmul_ru(E1, P1)),
-                                           __fmul_ru(0x1p-44f * QM, QM))));
-  const float D = __fadd_ru(fmaxf(fmaxf(fmaxf(fabsf(d1), fabsf(d2)), fmaxf(fabsf(d3), fabsf(d4))),
-                                  fmaxf(fabsf(d5), fabsf(d6))),
-                            err_d);
-  const float err_v = __fmul_ru(1.01f, __fadd_ru(__fadd_ru(__fmul_ru(4.f * D, err_d), 2.f * err_d * err_d),
-                                                 __fmul_ru(0x1p-22f, __fmul_ru(D, D))));
-  const float err_s = __fmul_ru(1.01f, __fadd_ru(2.f * err_d, __fmul_ru(0x1p-23f, D)));
-  auto clear = [&](float x, float e) { return fabsf(x) > __fadd_ru(2.f * e, 2.f * EPS); };
-  return clear(d1, err_d) && clear(d2, err_d) && clear(d3, err_d) && clear(d4, err_d) && clear(d5, err_d) &&
-         clear(d6, err_d) && clear(d4 - d3, err_s) && clear(d5 - d6, err_s) && clear(d1 - d3, err_s) &&
-         clear(vc, err_v) && clear(vb, err_v) && clear(va, err_v);
-}
-
-// Squared point-triangle distance in FP32 by Voronoi regions (Ericson,
-// Real-Time Collision Detection 5.1.5), measured from P; off receives P - cp,
-// the offset from the closest point.  The region tests run in Ericson's order
-// and each region keeps its formula, but the results are selected instead of
-// branched to, so that the lanes of a warp testing different triangles do not
-// diverge.  One division serves every region (its operands are selected); the
-// offset is base - v e1 - w e2 with fused operations.  kind receives the
-// region: 0 a vertex, 1 the edge AB or AC, 2 the edge BC or the face.
-__device__ __forceinline__ float dist2_f32_flat(const float* P, const float* A, const float* B, const float* C,
-                                               float* off, int& kind)
-{
-  const float ab0 = B[0] - A[0], ab1 = B[1] - A[1], ab2 = B[2] - A[2];
-  const float ac0 = C[0] - A[0], ac1 = C[1] - A[1], ac2 = C[2] - A[2];
-  const float bc0 = C[0] - B[0], bc1 = C[1] - B[1], bc2 = C[2] - B[2];
-  const float ap0 = P[0] - A[0], ap1 = P[1] - A[1], ap2 = P[2] - A[2];
-  const float bp0 = P[0] - B[0], bp1 = P[1] - B[1], bp2 = P[2] - B[2];
-  const float cp0 = P[0] - C[0], cp1 = P[1] - C[1], cp2 = P[2] - C[2];
-  const float d1 = dot3f(ab0, ap0, ab1, ap1, ab2, ap2);
-  const float d2 = dot3f(ac0, ap0, ac1, ap1, ac2, ap2);
-  const float d3 = dot3f(ab0, bp0, ab1, bp1, ab2, bp2);
-  const float d4 = dot3f(ac0, bp0, ac1, bp1, ac2, bp2);
-  const float d5 = dot3f(ab0, cp0, ab1, cp1, ab2, cp2);
-  const float d6 = dot3f(ac0, cp0, ac1, cp1, ac2, cp2);
-  const float vc = __fmaf_rn(d1, d4, -(d3 * d2));
-  const float vb = __fmaf_rn(d5, d2, -(d1 * d6));
-  const float va = __fmaf_rn(d3, d6, -(d5 * d4));
-  const bool rA = d1 <= 0.f && d2 <= 0.f;
-  const bool rB = !rA && d3 >= 0.f && d4 <= d3;
-  const bool rAB = !rA && !rB && vc <= 0.f && d1 >= 0.f && d3 <= 0.f;
-  const bool rC = !rA && !rB && !rAB && d6 >= 0.f && d5 <= d6;
-  const bool rAC = !rA && !rB && !rAB && !rC && vb <= 0.f && d2 >= 0.f && d6 <= 0.f;
-  const bool rBC = !rA && !rB && !rAB && !rC && !rAC && va <= 0.f && (d4 - d3) >= 0.f && (d5 - d6) >= 0.f;
-  const bool rF = !rA && !rB && !rAB && !rC && !rAC && !rBC;
-  kind = (rA || rB || rC) ? 0 : (rAB || rAC) ? 1 : 2;
-  const float num = rAB ? d1 : rAC ? d2 : rBC ? (d4 - d3) : 1.f;
-  const float den = rAB ? (d1 - d3) : rAC ? (d2 - d6) : rBC ? ((d4 - d3) + (d5 - d6)) : rF ? (va + vb + vc) : 1.f;
-  const float t = num / den;
-  const float v = rAB ? t : rF ? vb * t : 0.f;
-  const float w = (rAC || rBC) ? t : rF ? vc * t : 0.f;
-  // base and directions per region: A, AB, AC, face from A; B, BC from B; C from C
-  const bool fromB = rB || rBC, fromC = rC;
-  const float b0 = fromB ? bp0 : fromC ? cp0 : ap0, b1 = fromB ? bp1 : fromC ? cp1 : ap1,
-              b2 = fromB ? bp2 : fromC ? cp2 : ap2;
-  const float e0 = rBC ? bc0 : ac0, e1 = rBC ? bc1 : ac1, e2 = rBC ? bc2 : ac2;
-  off[0] = __fmaf_rn(-w, e0, __fmaf_rn(-v, ab0, b0));
-  off[1] = __fmaf_rn(-w, e1, __fmaf_rn(-v, ab1, b1));
-  off[2] = __fmaf_rn(-w, e2, __fmaf_rn(-v, ab2, b2));
-  return dot3f(off[0], off[0], off[1], off[1], off[2], off[2]);
-}
-
-// Per-query constants of the FP32 certificates.
-struct QCtx
-{
-  float qf[3];           // the point rounded to nearest
-  float eq;              // bound on the point's rounding (per axis)
-  float lip;             // coordinate-rounding part of the triangle distance error
-  float t_true, t_false; // box predicate thresholds from the interval holding minSq
-  float thr_leaf;        // sqrt(upper end of that interval) + 1e-6, rounded up
-};
-
-__device__ __forceinline__ void qctx_init(QCtx& c, const double* q, float mesh_max)
-{
-  float qabs = 0.f;
-  for(int d = 0; d < 3; ++d)
-  {
-    c.qf[d] = __double2float_rn(q[d]);
-    qabs = fmaxf(qabs, fabsf(c.qf[d]));
-  }
-  // |qf - q| <= 2^-24 |qf| (round to nearest; the absolute term covers
-  // subnormals); the subtraction in a gap is exact or contributes at most
-  // 2^-24 of the gap, which the relative term of box_decide covers
-  c.eq = __fadd_ru(__fmul_ru(0x1p-24f, qabs), 0x1p-149f);
-  // the point-triangle distance is 1-Lipschitz in the point and the vertices
-  c.lip = __fmul_ru(0x1p-21f, __fadd_ru(qabs, mesh_max));
-}
-
-// Thresholds for an exact minimum known to lie in the FP32 interval [lo, hi]:
-// t_true <= minSq (1 - 2^-40) and t_false >= minSq (1 + 2^-40) with room for
-// the FP64 predicate's own rounding; thr_leaf >= sqrt(minSq) + 1e-6.  No FP64
-// arithmetic.
-__device__ __forceinline__ void qctx_set32(QCtx& c, float lo, float hi)
-{
-  c.t_true = __fmul_rd(lo, 1.f - 0x1p-22f);
-  c.t_false = __fmul_ru(hi, 1.f + 0x1p-22f);
-  c.thr_leaf = __fadd_ru(__fsqrt_ru(hi), 1.0001e-6f);
-}
-
-// The same for an exactly known FP64 minimum.
-__device__ __forceinline__ void qctx_update(QCtx& c, double minSq)
-{
-  qctx_set32(c, __double2float_rd(minSq), __double2float_ru(minSq));
-}
-
 // squared_distance(p, box) <= minSq decided in FP32 (SD:576-578).  s is the
 // per-axis signed gap to the outward-rounded box in round-to-nearest (> 0
 // outside); it differs from the exact signed gap to the FP64 box by at most
@@ -327,51 +170,19 @@ __device__ __forceinline__ int leaf_prefilter(const LeafRec32<NPC>* __restrict__
     int kind;
     const float d2 = dist2_f32_flat(c.qf, A, B, C, off, kind);
     const float ap = fmaxf(fabsf(c.qf[0] - A[0]), fmaxf(fabsf(c.qf[1] - A[1]), fabsf(c.qf[2] - A[2])));
-    const float E = __fadd_ru(c.lip, __fmul_ru(ec[s], __fadd_ru(ap, lt[s])));
+    // the general error of tri_bounds (kappa^2 growth for slivers included)
+    const float E =
+        __fadd_ru(c.lip, __fmul_ru(__fmul_ru(ec[s], fmaxf(1.f, ec[s] * 65536.f * 0.0625f)), __fadd_ru(ap, lt[s])));
     const float lim = __fadd_ru(c.thr_leaf, E);
     if(!(d2 > __fmul_ru(__fmul_ru(lim, lim), 1.0f + 0x1p-20f))) need |= 1 << s;
   }
   return need;
 }
 
-// Error of the FP32 distance sqrt(d2) = sd of dist2_f32_flat when its region
-// is certain (crisp_regions) and not the edge BC or the face.  u = 2^-24.
-// Rounding the point and the vertices moves the exact distance by at most
-// u sqrt(3) (|q|_inf + M) (it is 1-Lipschitz in them), below lip / 4.
-//  * vertex V: off = fl(qf - Vf) exactly as the offset, within u |off| of
-//    qf - Vf: sd is within lip / 4 + 2^-23 sd of |q - V|, and the FP64 point
-//    is V itself;
-//  * edge AB (AC alike): t = d1 / (d1 - d3) and off = fl(ap - t ab).  With
-//    dots of rounded differences within 5.01 u |e| |p| of the exact ones,
-//    |t - t*| <= 5.1 u (2 |ap| + |bp|) / |ab| + 2 u to first order, and
-//    |off - off*| <= u (|off| + 16.3 |ap|_2 + 8.1 |ab|) with |ap|_2 <=
-//    sqrt(3) ap (ap the largest coordinate of qf - A) and |ab| <= lt:
-//    lip / 4 + 2^-23 sd + 2^-19 ap + 2^-20 lt.  First order holds while the
-//    relative error of d1 - d3 is small: every edge is at least lt / kappa
-//    long (kappa = ec 2^16), so ap ec <= lt / 16 keeps |ap|_2 / |ab| below
-//    7100 and that error below 1/200, which the constants' margins cover.
-// The FP64 routine's point is within 2^-36 M of the exact projection, far
-// inside either bound.  Returns +inf where no bound applies.
-__device__ __forceinline__ float region_error(int kind, float lip, float sd, float ap, float lt, float ec)
-{
-  const float base = __fadd_ru(__fmul_ru(0.25f, lip), __fmul_ru(0x1p-23f, sd));
-  if(kind == 0) return base;
-  if(kind == 1 && __fmul_ru(ap, ec) <= 0.0625f * lt)
-    return __fadd_ru(base, __fadd_ru(__fmul_ru(0x1p-19f, ap), __fmul_ru(0x1p-20f, lt)));
-  return INFINITY;
-}
-
 // leaf_prefilter that also bounds, for the triangles it keeps, the squared
-// distance the FP64 checkCandidate will compute: [lo2, hi2] holds the minimum
-// over the kept triangles.  The FP64 point always lies on the triangle, so the
-// lower end needs only the FP32 error.  The upper end adds the FP64 routine's
-// own departure from the exact closest point: its fuzzy region tests
-// (closest_point.hpp:181-282) use a fixed EPS = 1e-12 on dot products
-// (length^2), which moves the point by at most 1e-12 / (shortest edge)
-// <= 1e-12 kappa / L, and on the products vc, vb, va (length^4), which moves
-// it by at most 1e-12 / (edge |n|) <= 1e-12 kappa^2 / L^3 (for the small
-// triangles of fine meshes this is ~1e-6, far above rounding); both doubled.
-// mesh_max bounds the mesh's coordinates (rounded up).
+// distance the FP64 checkCandidate will compute (tri_bounds): [lo2, hi2] holds
+// the minimum over the kept triangles, cpf and rad the last kept one's closest
+// point estimate and its radius.  mesh_max bounds the mesh's coordinates.
 template <int NPC>
 __device__ __forceinline__ int leaf_prefilter_bounds(const LeafRec32<NPC>* __restrict__ leaves32, int leafpos,
                                                      const QCtx& c, float mesh_max, float& lo2, float& hi2, float* cpf,
@@ -401,51 +212,17 @@ __device__ __forceinline__ int leaf_prefilter_bounds(const LeafRec32<NPC>* __res
 #pragma unroll
   for(int s = 0; s < NPC - 2; ++s)
   {
-    const float* A = v;
-    const float* B = v + 3 * (s + 1);
-    const float* C = v + 3 * (s + 2);
-    float off[3];
-    int kind;
-    const float d2 = dist2_f32_flat(c.qf, A, B, C, off, kind);
-    const float ap = fmaxf(fabsf(c.qf[0] - A[0]), fmaxf(fabsf(c.qf[1] - A[1]), fabsf(c.qf[2] - A[2])));
-    float E = __fadd_ru(c.lip, __fmul_ru(ec[s], __fadd_ru(ap, lt[s])));
-    const float lim = __fadd_ru(c.thr_leaf, E);
-    if(!(d2 > __fmul_ru(__fmul_ru(lim, lim), 1.0f + 0x1p-20f)))
+    float d2, l2, h2;
+    if(tri_bounds<NPC == 4>(c, mesh_max, v, v + 3 * (s + 1), v + 3 * (s + 2), ec[s], lt[s], fzt, d2, l2, h2, cpf, rad))
     {
       need |= 1 << s;
-      float fz;
-      if constexpr(NPC == 3)
-        fz = fzt;  // stored with the triangle
-      else
-      {
-        const float kappa = ec[s] * (1.f / (256.f * 0x1p-24f));
-        const float kl = __fdiv_ru(kappa, lt[s]);
-        fz = __fmul_ru(2e-12f, __fadd_ru(kl, __fdiv_ru(__fmul_ru(kl, kl), lt[s])));
-      }
-      // sqrt(d2 (1 -+ 2^-20)) from the correctly rounded sqrt(d2): the factor
-      // 1 -+ 2^-20 covers both the 2^-21 of the square root of the margin and
-      // the 2^-24 rounding of sqrtf
-      const float sd = sqrtf(d2);
-      // no fuzzy displacement when every region test is clear of its EPS band;
-      // the region is then certain, and a vertex or an edge at A has a
-      // tighter error than the general one
-      // (eq 2^24 bounds the point's largest coordinate)
-      if(crisp_regions(c.qf, A, B, C, c.eq * 0x1p24f, mesh_max))
-      {
-        fz = 0.f;
-        E = fminf(E, region_error(kind, c.lip, sd, ap, lt[s], ec[s]));
-      }
-      const float dl = fmaxf(__fsub_rd(__fmul_rd(sd, 1.f - 0x1p-20f), E), 0.f);
-      const float dh = __fadd_ru(__fadd_ru(__fmul_ru(sd, 1.f + 0x1p-20f), E), fz);
-      const float l2 = __fmul_rd(dl, dl), h2 = __fmul_ru(dh, dh);
       lo2 = (d2 == d2) ? fminf(lo2, l2) : 0.f;
       hi2 = (d2 == d2 && h2 == h2) ? fminf(hi2, h2) : hi2;
-      // closest point estimate: the exact projection is 1-Lipschitz, so the
-      // FP64 point lies within 2 (E + fz) of qf - off
-      for(int d = 0; d < 3; ++d) cpf[d] = c.qf[d] - off[d];
-      rad = __fmul_ru(2.f, __fadd_ru(E, fz));
     }
   }
+  // both triangles of a quad kept: either may set the closest point, and
+  // cpf is only the second one's, so nothing may be certified far from it
+  if(need == 3) rad = INFINITY;
   return need;
 }
 
