@@ -43,29 +43,7 @@ __global__ void k_nodes32(const NodeRec64* __restrict__ in, int n_inner, NodeRec
   NodeRec32 r;
   for(int side = 0; side < 2; ++side)
   {
-    const double* b = in[i].b + 6 * side;
-    float* o = r.b + 6 * side;
-    float slack = 0.f;
-    if(!box_valid(b, b + 3))
-    {
-      for(int d = 0; d < 3; ++d)
-      {
-        o[d] = INFINITY;
-        o[3 + d] = -INFINITY;
-      }
-    }
-    else
-    {
-      double s = 0.0;
-      for(int d = 0; d < 3; ++d)
-      {
-        o[d] = __double2float_rd(b[d]);
-        o[3 + d] = __double2float_ru(b[3 + d]);
-        s = fmax(s, fmax(b[d] - (double)o[d], (double)o[3 + d] - b[3 + d]));
-      }
-      slack = (s == s) ? __double2float_ru(s) : INFINITY;
-    }
-    r.pad[side] = __float_as_int(slack);
+    r.pad[side] = __float_as_int(node_box32(in[i].b + 6 * side, r.b + 6 * side));
   }
   r.child[0] = in[i].child[0];
   r.child[1] = in[i].child[1];

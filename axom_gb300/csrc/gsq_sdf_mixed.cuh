@@ -45,48 +45,8 @@ struct MeshInfo
 
 namespace sdf
 {
-// squared_distance(p, box) <= minSq decided in FP32 (SD:576-578).  s is the
-// per-axis signed gap to the outward-rounded box in round-to-nearest (> 0
-// outside); it differs from the exact signed gap to the FP64 box by at most
-// del = slack + eq plus 2^-24 |s|.  An axis with s < -del (plus that term) has
-// an exact gap of 0 and contributes no error; the others contribute
-// 2 del g + del^2, and 2^-21 sum g^2 covers the relative terms and the FP32
-// rounding of the sum.  0: certainly false, 1: certainly true, 2: undecided.
-__device__ __forceinline__ int box_decide(const float* lo, const float* hi, float slack, const QCtx& c)
-{
-  const float del = slack + c.eq;
-  const float s0 = fmaxf(lo[0] - c.qf[0], c.qf[0] - hi[0]);
-  const float s1 = fmaxf(lo[1] - c.qf[1], c.qf[1] - hi[1]);
-  const float s2 = fmaxf(lo[2] - c.qf[2], c.qf[2] - hi[2]);
-  const float g0 = fmaxf(s0, 0.f), g1 = fmaxf(s1, 0.f), g2 = fmaxf(s2, 0.f);
-  const float lim = -1.01f * del;
-  const float n0 = (s0 * 0.999f < lim) ? 0.f : 1.f;
-  const float n1 = (s1 * 0.999f < lim) ? 0.f : 1.f;
-  const float n2 = (s2 * 0.999f < lim) ? 0.f : 1.f;
-  const float d2 = dot3f(g0, g0, g1, g1, g2, g2);
-  const float err = __fmaf_rn(0x1p-21f, d2, __fmaf_rn(1.01f * del * del, n0 + n1 + n2, 2.02f * del * (g0 + g1 + g2)));
-  if(!(err < INFINITY)) return 2;
-  if(__fsub_rd(d2, err) > c.t_false) return 0;
-  if(__fadd_ru(d2, err) <= c.t_true) return 1;
-  return 2;
-}
-
-// One node visit decided in FP32.  Returns false if some decision is not
-// certain (the caller then decides the whole visit in FP64 with visit_fp64).
-// The child order (the nearer centroid first, LinearBVH.hpp:72-85) is the
-// sign of 4 (|c_L - q|^2 - |c_R - q|^2) = sum_d a_d b_d, built from the gaps
-// lo - q and q - hi the box tests use: per child u = (lo - q) - (q - hi) =
-// 2 (c - q), a = u_L - u_R, b = u_L + u_R.  Against the exact values of the
-// FP64 boxes and point, per axis (r the sum of the four |gaps|, s_L, s_R the
-// boxes' rounding slacks, eq the point's):
-//   |da| <= 2 (s_L + s_R) + 2^-22 r          (the point cancels in a)
-//   |db| <= 2 (s_L + s_R) + 4 eq + 2^-22 r
-// (three roundings of at most 2^-24 of a gap sum each), so the dot is within
-//   (c0 + 4 eq) A1 + c0 B1 + 2^-22 sum r (|a| + |b|) + 2^-21 sum |a b|
-//   + 6 (c0 + 4 eq)^2 + 2^-43 sum r^2,      c0 = 2 (s_L + s_R),
-// A1 = sum |a|, B1 = sum |b| (the fused dot rounds three times).  The FP64
-// comparison of the rounded centroids' squared distances is within
-// 2^-50 Mq sum r (Mq the largest coordinate, below 2^21 lip) of the exact one.
+// One node visit of record cur decided in FP32 (visit32_core on its two child
+// boxes and slacks); ch receives the record's child links.
 __device__ __forceinline__ bool visit32(const NodeRec32* __restrict__ nodes32, int cur, const QCtx& c, bool& inL,
                                         bool& inR, bool& swap, int2& ch)
 {
@@ -96,45 +56,7 @@ __device__ __forceinline__ bool visit32(const NodeRec32* __restrict__ nodes32, i
   ch = make_int2(lk.x, lk.y);
   const float lo_l[3] = {a.x, a.y, a.z}, hi_l[3] = {a.w, b.x, b.y};
   const float lo_r[3] = {b.z, b.w, cc.x}, hi_r[3] = {cc.y, cc.z, cc.w};
-  const float sl_ = __int_as_float(lk.z), sr_ = __int_as_float(lk.w);
-  // an invalid box is stored as [+inf, -inf]: its gap is +inf, box_decide
-  // leaves it undecided and the FP64 visit applies the validity rule
-  const int dl = box_decide(lo_l, hi_l, sl_, c);
-  const int dr = box_decide(lo_r, hi_r, sr_, c);
-  if(dl == 2 || dr == 2) return false;
-  swap = false;
-  if(dl == 1 && dr == 1)
-  {
-    float dot = 0.f, A1 = 0.f, B1 = 0.f, es = 0.f, rr = 0.f, R1 = 0.f, prod = 0.f;
-#pragma unroll
-    for(int d = 0; d < 3; ++d)
-    {
-      const float gll = lo_l[d] - c.qf[d], ghl = c.qf[d] - hi_l[d];
-      const float glr = lo_r[d] - c.qf[d], ghr = c.qf[d] - hi_r[d];
-      const float uL = gll - ghl, uR = glr - ghr;
-      const float av = uL - uR, bv = uL + uR;
-      dot = __fmaf_rn(av, bv, dot);
-      const float aa = fabsf(av), bb = fabsf(bv);
-      const float r = (fabsf(gll) + fabsf(ghl)) + (fabsf(glr) + fabsf(ghr));
-      A1 += aa;
-      B1 += bb;
-      R1 += r;
-      es = __fmaf_rn(r, aa + bb, es);
-      rr = __fmaf_rn(r, r, rr);
-      prod = __fmaf_rn(aa, bb, prod);
-    }
-    const float c0 = 2.f * (sl_ + sr_), c04 = c0 + 4.f * c.eq;
-    const float bound = 1.02f * (c04 * A1 + c0 * B1 + 0x1p-22f * es + 0x1p-21f * prod + 6.f * c04 * c04 +
-                                 0x1p-43f * rr + 0x1p-29f * c.lip * R1);
-    if(!(bound < INFINITY)) return false;
-    if(dot > bound)
-      swap = true;
-    else if(!(dot < -bound))
-      return false;
-  }
-  inL = (dl == 1);
-  inR = (dr == 1);
-  return true;
+  return visit32_core(lo_l, hi_l, lo_r, hi_r, __int_as_float(lk.z), __int_as_float(lk.w), c, inL, inR, swap);
 }
 
 // FP32 certificate of the leaf action: bit s of the result is set when
