@@ -111,6 +111,22 @@ def displaced_icosphere(level: int, seed: int = 1234) -> tuple[np.ndarray, np.nd
     return displace(v, seed), f
 
 
+def sliver_sheet(seed: int, n: int = 40) -> tuple[np.ndarray, np.ndarray]:
+    """An open jittered grid surface with many slivers; every 17th triangle is
+    collapsed onto a line (zero area)."""
+    g = rng(seed)
+    x, y = np.meshgrid(np.linspace(0, 1, n), np.linspace(0, 1, n), indexing="ij")
+    z = 0.05 * np.sin(6 * x) * np.cos(5 * y)
+    v = np.stack([x, y, z], -1).reshape(-1, 3)
+    v[:, :2] += g.normal(scale=0.004, size=(v.shape[0], 2))
+    i, j = np.meshgrid(np.arange(n - 1), np.arange(n - 1), indexing="ij")
+    a = (i * n + j).ravel()
+    f = np.concatenate([np.stack([a, a + n, a + n + 1], 1), np.stack([a, a + n + 1, a + 1], 1)]).astype(np.int32)
+    deg = f[::17]
+    v[deg[:, 2]] = 0.5 * (v[deg[:, 0]] + v[deg[:, 1]])
+    return v, f
+
+
 def expanded_box(v: np.ndarray, factor: float = 1.2) -> tuple[np.ndarray, np.ndarray]:
     lo, hi = v.min(axis=0), v.max(axis=0)
     c, h = 0.5 * (lo + hi), 0.5 * (hi - lo) * factor

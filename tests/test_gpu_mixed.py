@@ -30,25 +30,6 @@ def test_mixed_matches_golden(gsq, name):
     np.testing.assert_allclose(nr, g["normals"], rtol=0, atol=1e-12)
 
 
-def sliver_mesh(seed: int):
-    """A jittered grid surface with many slivers and some zero-area triangles."""
-    rng = np.random.default_rng(seed)
-    n = 40
-    x, y = np.meshgrid(np.linspace(0, 1, n), np.linspace(0, 1, n), indexing="ij")
-    z = 0.05 * np.sin(6 * x) * np.cos(5 * y)
-    v = np.stack([x, y, z], -1).reshape(-1, 3)
-    v[:, :2] += rng.normal(scale=0.004, size=(v.shape[0], 2))
-    i, j = np.meshgrid(np.arange(n - 1), np.arange(n - 1), indexing="ij")
-    a = (i * n + j).ravel()
-    f = np.concatenate([np.stack([a, a + n, a + n + 1], 1), np.stack([a, a + n + 1, a + 1], 1)])
-    # collapse some triangles onto a line (zero area) and squash others into slivers
-    v2 = v.copy()
-    f = f.astype(np.int32)
-    deg = f[::17]
-    v2[deg[:, 2]] = 0.5 * (v2[deg[:, 0]] + v2[deg[:, 1]])
-    return v2, f
-
-
 @pytest.mark.parametrize("case", ["ico5", "ico6", "quad30", "slivers", "open_ico5"])
 def test_mixed_equals_fp64_with_audit(gsq, case):
     watertight = True
@@ -58,7 +39,7 @@ def test_mixed_equals_fp64_with_audit(gsq, case):
         v, f = W.quad_sphere(30)
         v = W.displace(v, 8)
     elif case == "slivers":
-        v, f = sliver_mesh(3)
+        v, f = W.sliver_sheet(3)
         watertight = False
     else:
         v, f = W.displaced_icosphere(5, 9)

@@ -175,6 +175,40 @@ def test_port_matches_reference_sdf_live(port, ref):
         assert_bits_equal(a[2], b[2], "normals")
 
 
+def _on_features(v, f):
+    """Points exactly on vertices, edge midpoints and centroids of the cells."""
+    a, b, c = v[f[:, 0]], v[f[:, 1]], v[f[:, 2]]
+    return np.concatenate([v, 0.5 * (a + b), 0.5 * (b + c), (a + b + c) / 3.0])
+
+
+@pytest.mark.parametrize("case", ["slivers", "quads", "tiny1", "tiny2", "empty"])
+def test_port_matches_reference_sdf_edge_cases(port, ref, case):
+    """Slivers and zero-area triangles (open surface), quad cells, meshes of
+    0, 1 and 2 triangles (BVH padding; an empty mesh gives sqrt(DBL_MAX)),
+    points exactly on vertices, edges and faces and far away, every
+    watertight / sign combination."""
+    if case == "slivers":
+        v, f = W.sliver_sheet(3)
+    elif case == "quads":
+        v, f = W.quad_sphere(12)
+        v = W.displace(v, 8)
+    else:
+        v = np.array([[0.0, 0, 0], [1, 0, 0], [0, 1, 0], [1, 1, 0.5]])
+        f = {"tiny1": [[0, 1, 2]], "tiny2": [[0, 1, 2], [1, 3, 2]], "empty": np.zeros((0, 3))}[case]
+        f = np.asarray(f, np.int32)
+    pts = [W.uniform_queries(v, 2000, 1), W.uniform_queries(v, 200, 2, factor=40.0)]
+    if f.shape[0]:
+        pts.append(_on_features(v, f[:, :3])[:: max(1, v.shape[0] // 500)])
+    q = np.concatenate(pts)
+    for wt, sg in ((True, True), (False, True), (True, False), (False, False)):
+        hp = port.sdf(v[:, 0], v[:, 1], v[:, 2], f, wt, sg)
+        hr = ref.sdf(v[:, 0], v[:, 1], v[:, 2], f, wt, sg)
+        a = port.sdf_eval(hp, q, True, True)
+        b = ref.sdf_eval(hr, q, True, True)
+        for x, y, what in zip(a, b, ("distance", "closest", "normals")):
+            assert_bits_equal(x, y, f"{case} {what} (watertight {wt}, sign {sg})")
+
+
 @pytest.mark.parametrize("tag", ["all", "thr"])
 def test_port_closest_point_matches_golden(port, tag):
     """DistributedClosestPoint's local query against the reference's outputs."""
