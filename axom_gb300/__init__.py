@@ -125,6 +125,25 @@ SIGNATURES = [
     ("gsq_batch_set_opts", C.c_int, [_vp, _vp]),
     ("gsq_batch_last_ms", C.c_int, [_vp, C.POINTER(C.c_float)]),
     ("gsq_batch_max_depth", C.c_int, [_vp, _ip]),
+    # the quest C interface (include/gsq_quest.h)
+    ("QUEST_signed_distance_init_serial", C.c_int, [C.c_char_p]),
+    ("QUEST_signed_distance_init_serial_bufferify", C.c_int, [C.c_char_p, C.c_int]),
+    ("QUEST_signed_distance_initialized", C.c_bool, []),
+    ("QUEST_signed_distance_get_mesh_bounds", None, [_dp, _dp]),
+    ("QUEST_signed_distance_set_dimension", None, [C.c_int]),
+    ("QUEST_signed_distance_set_closed_surface", None, [C.c_bool]),
+    ("QUEST_signed_distance_set_compute_signs", None, [C.c_bool]),
+    ("QUEST_signed_distance_set_allocator", None, [C.c_int]),
+    ("QUEST_signed_distance_set_verbose", None, [C.c_bool]),
+    ("QUEST_signed_distance_use_shared_memory", None, [C.c_bool]),
+    ("QUEST_signed_distance_set_execution_space", None, [C.c_int]),
+    ("QUEST_signed_distance_evaluate_0", C.c_double, [C.c_double, C.c_double, C.c_double]),
+    ("QUEST_signed_distance_evaluate_1", C.c_double, [C.c_double, C.c_double, C.c_double] + [_dp] * 6),
+    ("QUEST_signed_distance_finalize", None, []),
+    ("gsq_quest_init_mesh", C.c_int, [_vp, _vp, _vp, C.c_int32, _vp, C.c_int32]),
+    ("gsq_quest_evaluate_points", None, [_vp, _vp, _vp, C.c_int32, _vp]),
+    ("gsq_quest_set_precision", C.c_int, [C.c_int32]),
+    ("gsq_quest_handle", C.c_int, [C.POINTER(_vp)]),
 ]
 NOALLOC_MAX_QUERIES = 262144  # GSQ_NOALLOC_MAX_QUERIES in include/gsq.h
 

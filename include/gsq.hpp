@@ -19,6 +19,7 @@
 #include <vector>
 
 #include "gsq.h"
+#include "gsq_quest.h"
 
 namespace gsq
 {
@@ -300,6 +301,58 @@ private:
   gsq_cpq* m_h = nullptr;
   double m_sq_threshold = DBL_MAX;
 };
+
+// The C-style interface of quest/interface/signed_distance.hpp:88-319 (a
+// global query object), over the QUEST_signed_distance_* entry points of
+// gsq_quest.h.  As in the reference, misuse (options after init, evaluate
+// before init, null buffers, a dimension other than 3) aborts the process.
+enum class SignedDistExec
+{
+  CPU = QUEST_SignedDistExec_CPU,
+  OpenMP = QUEST_SignedDistExec_OpenMP,
+  GPU = QUEST_SignedDistExec_GPU
+};
+
+// signed_distance_init(file) (signed_distance.hpp:117) and (mesh) (:137): 0, or -1
+inline int signed_distance_init(const std::string& file) { return QUEST_signed_distance_init_serial(file.c_str()); }
+inline int signed_distance_init(const SurfaceMesh* m)
+{
+  // triangles only: -1 for other cells, where the reference aborts
+  // (signed_distance.cpp:174-175)
+  if(m->nodes_per_cell != 3) return -1;
+  return gsq_quest_init_mesh(m->x.data(), m->y.data(), m->z.data(), (int32_t)m->x.size(), m->cells.data(),
+                             m->numCells());
+}
+inline bool signed_distance_initialized() { return QUEST_signed_distance_initialized(); }
+inline void signed_distance_set_dimension(int dim) { QUEST_signed_distance_set_dimension(dim); }
+inline void signed_distance_set_closed_surface(bool status) { QUEST_signed_distance_set_closed_surface(status); }
+inline void signed_distance_set_compute_signs(bool computeSign)
+{
+  QUEST_signed_distance_set_compute_signs(computeSign);
+}
+inline void signed_distance_set_allocator(int allocatorID) { QUEST_signed_distance_set_allocator(allocatorID); }
+inline void signed_distance_set_verbose(bool status) { QUEST_signed_distance_set_verbose(status); }
+inline void signed_distance_use_shared_memory(bool status) { QUEST_signed_distance_use_shared_memory(status); }
+inline void signed_distance_set_execution_space(SignedDistExec s)
+{
+  QUEST_signed_distance_set_execution_space((int)s);
+}
+// signed_distance_evaluate (:248, :266, :290)
+inline double signed_distance_evaluate(double x, double y, double z = 0.0)
+{
+  return QUEST_signed_distance_evaluate_0(x, y, z);
+}
+inline double signed_distance_evaluate(double x, double y, double z, double& cp_x, double& cp_y, double& cp_z,
+                                       double& n_x, double& n_y, double& n_z)
+{
+  return QUEST_signed_distance_evaluate_1(x, y, z, &cp_x, &cp_y, &cp_z, &n_x, &n_y, &n_z);
+}
+inline void signed_distance_evaluate(const double* x, const double* y, const double* z, int npoints, double* phi)
+{
+  gsq_quest_evaluate_points(x, y, z, npoints, phi);
+}
+inline void signed_distance_get_mesh_bounds(double* lo, double* hi) { QUEST_signed_distance_get_mesh_bounds(lo, hi); }
+inline void signed_distance_finalize() { QUEST_signed_distance_finalize(); }
 }  // namespace quest
 }  // namespace gsq
 

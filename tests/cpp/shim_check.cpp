@@ -93,6 +93,33 @@ int main()
     std::remove(path);
   }
 
+  // the C-style interface with a mesh (quest_signed_distance_interface.cpp:
+  // 372-404 bounds, 186-242 plane values): init, evaluate in the three
+  // forms, bounds, finalize
+  {
+    EXPECT(!gsq::quest::signed_distance_initialized());
+    gsq::quest::signed_distance_set_closed_surface(false);
+    gsq::quest::signed_distance_set_execution_space(gsq::quest::SignedDistExec::GPU);
+    EXPECT(gsq::quest::signed_distance_init(&plane) == 0);
+    EXPECT(gsq::quest::signed_distance_initialized());
+    double xs[3] = {0.5, -3.0, 4.0}, ys[3] = {-1.25, 2.0, 4.0}, zs[3] = {2.0, -0.75, 3.5}, phi[3];
+    gsq::quest::signed_distance_evaluate(xs, ys, zs, 3, phi);
+    for(int i = 0; i < 3; ++i)
+    {
+      EXPECT(std::fabs(phi[i] - zs[i]) <= 4 * 2.220446049250313e-16 * std::fabs(zs[i]));
+      EXPECT(gsq::quest::signed_distance_evaluate(xs[i], ys[i], zs[i]) == phi[i]);
+      double cx, cy, cz, nx, ny, nz;
+      EXPECT(gsq::quest::signed_distance_evaluate(xs[i], ys[i], zs[i], cx, cy, cz, nx, ny, nz) == phi[i]);
+      EXPECT(std::fabs(cx - xs[i]) <= 1e-12 && std::fabs(cy - ys[i]) <= 1e-12 && std::fabs(cz) <= 1e-12);
+      EXPECT(std::fabs(nz - 1.0) <= 1e-12);
+    }
+    double lo[3], hi[3];
+    gsq::quest::signed_distance_get_mesh_bounds(lo, hi);
+    EXPECT(lo[0] == -5 && lo[1] == -5 && lo[2] == 0 && hi[0] == 5 && hi[1] == 5 && hi[2] == 0);
+    gsq::quest::signed_distance_finalize();
+    EXPECT(!gsq::quest::signed_distance_initialized());
+  }
+
   // closest object point: the 27 cell corners (0..3)^3 minus one
   {
     std::vector<gsq::Point> pts;

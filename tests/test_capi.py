@@ -26,7 +26,7 @@ def declared_functions() -> list[str]:
     names = []
     for h in (ROOT / "include").glob("*.h"):
         text = re.sub(r"/\*.*?\*/", "", h.read_text(), flags=re.S)
-        names += re.findall(r"^\s*(?:const\s+)?\w+\**\s+\**(gsq_\w+)\s*\(", text, flags=re.M)
+        names += re.findall(r"^\s*(?:const\s+)?\w+\**\s+\**((?:gsq|QUEST)_\w+)\s*\(", text, flags=re.M)
     return sorted(set(names))
 
 
