@@ -162,6 +162,36 @@ def test_port_matches_reference_edge_cases(port, ref):
                 assert_bits_equal(x, y, "find boxes")
 
 
+def test_port_matches_reference_points_and_rays_edge_cases(port, ref):
+    """findPoints with points on box corners, faces and inside, and findRays
+    with axis-aligned directions (zero components: infinite slab parameters),
+    zero directions, origins on corners and inside boxes, over boxes with
+    duplicates, flat and invalid ones, at both scale factors."""
+    rng = np.random.default_rng(11)
+    lo = rng.uniform(0, 1, (300, 3))
+    boxes = np.concatenate([lo, lo + rng.uniform(0, 0.25, (300, 3))], 1)
+    boxes = np.concatenate([boxes, np.tile(boxes[:1], (16, 1))])
+    boxes[::7, 2] = boxes[::7, 5]  # flat in z
+    boxes[5::11, [1, 4]] = boxes[5::11, [4, 1]]  # invalid in y
+    corners = np.concatenate([boxes[:60, :3], boxes[:60, 3:], np.stack([boxes[:60, 0], boxes[:60, 4],
+                                                                       boxes[:60, 2]], 1)])
+    faces = 0.5 * (boxes[:60, :3] + boxes[:60, 3:])
+    faces[:, 0] = boxes[:60, 0]
+    pts = np.concatenate([corners, faces, rng.uniform(-0.2, 1.2, (300, 3))])
+    axes = np.repeat(np.eye(3), 20, axis=0) * np.where(rng.uniform(size=(60, 1)) < 0.5, -1.0, 1.0)
+    dirs = np.concatenate([axes, np.zeros((5, 3)), rng.normal(size=(200, 3))])
+    origins = np.concatenate([corners[: len(axes)], faces[:5], rng.uniform(-0.5, 1.5, (200, 3))])
+    for scale in (1.000123, 1.0):
+        hp, hr = port.bvh(boxes, scale), ref.bvh(boxes, scale)
+        for x, y in zip(port.find_points(hp, pts), ref.find_points(hr, pts)):
+            assert_bits_equal(x, y, f"find points, scale {scale}")
+        *got, unit = ref.find_rays(hr, origins, dirs)
+        assert_bits_equal(port.normalize_rays(dirs), unit, "ray normalisation")
+        for x, y in zip(port.find_rays(hp, origins, unit), got):
+            assert_bits_equal(x, y, f"find rays, scale {scale}")
+        assert got[1].sum() > 100 and (got[1] == 0).any()  # hits and misses
+
+
 def test_port_matches_reference_sdf_live(port, ref):
     v, f = W.displaced_icosphere(4, 77)
     q = W.mixed_queries(v, f, 3000, 5)
