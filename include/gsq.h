@@ -5,7 +5,9 @@
  *   - spin::BVH<3, Exec, double>           (src/axom/spin/BVH.hpp:129-568)
  *   - quest::SignedDistance<3, Exec>       (src/axom/quest/SignedDistance.hpp:147-605)
  *   - the quest C API / shroud wrappers     (src/axom/quest/interface/signed_distance.hpp:88-319,
- *                                            src/axom/quest/interface/c_fortran/wrapQUEST.h:84-129)
+ *                                            src/axom/quest/interface/c_fortran/wrapQUEST.h:84-129;
+ *                                            their QUEST_signed_distance_* entry points themselves
+ *                                            are declared in gsq_quest.h)
  *
  * Conventions
  *   - Every function returns an int status: GSQ_OK (0) on success, a negative
