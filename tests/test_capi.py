@@ -102,3 +102,16 @@ def test_batch_argument_validation_without_gpu(lib):
                                 None) == -1
     assert lib.gsq_batch_run(None, None, None, None) == -1
     assert lib.gsq_batch_destroy(None) == 0
+
+
+def test_callers_compile_and_link(lib, tmp_path):
+    """The C++ shim caller and the C99 caller of the quest entry points compile
+    against include/ and link libgsq.so (they run in the GPU suite)."""
+    import subprocess
+    lib_dir = ROOT / "axom_gb300"
+    for src, cc in (("shim_check.cpp", ["g++", "-std=c++17"]), ("quest_check.c", ["gcc", "-std=c99"])):
+        exe = tmp_path / src.split(".")[0]
+        p = subprocess.run(cc + ["-O1", "-Wall", "-Werror", f"-I{ROOT / 'include'}", str(ROOT / "tests/cpp" / src),
+                                 f"-L{lib_dir}", "-lgsq", "-lm", f"-Wl,-rpath,{lib_dir}", "-o", str(exe)],
+                           capture_output=True, text=True)
+        assert p.returncode == 0, p.stderr
