@@ -103,3 +103,29 @@ def test_misuse_aborts_like_the_reference(call, message):
     assert "before" in p.stdout and "after" not in p.stdout, p.stdout + p.stderr
     assert p.returncode == -signal.SIGABRT, (p.returncode, p.stderr)
     assert message in p.stderr, p.stderr
+
+
+def test_python_module_mirrors_the_reference_module():
+    """axom_gb300.quest has the functions of the reference's Python module
+    (pyQUESTmodule.cpp:718-760); init fails with -1 on a missing file; an
+    evaluate before init aborts, as there."""
+    from axom_gb300 import quest
+    for name in ("signed_distance_init", "signed_distance_initialized", "signed_distance_set_dimension",
+                 "signed_distance_set_closed_surface", "signed_distance_set_compute_signs",
+                 "signed_distance_set_allocator", "signed_distance_set_verbose",
+                 "signed_distance_use_shared_memory", "signed_distance_set_execution_space",
+                 "signed_distance_evaluate", "signed_distance_finalize"):
+        assert callable(getattr(quest, name)), name
+    p = run_child("""
+        from axom_gb300 import quest
+        assert quest.signed_distance_init("badfile.stl") == -1
+        assert not quest.signed_distance_initialized()
+        quest.signed_distance_set_closed_surface(False)
+        quest.signed_distance_set_execution_space(quest.SignedDistExec_GPU)
+        quest.signed_distance_finalize()
+        print("before", flush=True)
+        quest.signed_distance_evaluate(0.0, 0.0, 0.0)
+        print("after")
+    """)
+    assert "before" in p.stdout and "after" not in p.stdout, p.stdout + p.stderr
+    assert p.returncode == -signal.SIGABRT and "must be initialized" in p.stderr, p.stderr
