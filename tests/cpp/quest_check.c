@@ -7,7 +7,9 @@
  * (EXPECT_DOUBLE_EQ, :186-242), with closest point (x, y, 0) and normal
  * (0, 0, 1); the mesh bounds are the nodes' (:372-404); finalize leaves the
  * query uninitialized; a second init as a closed, unsigned surface gives |z|.
- * Usage: quest_check <scratch STL path>.  Prints OK and exits 0 on success. */
+ * Usage: quest_check <scratch STL path> [misuse 0-7]; with a misuse case it
+ * prints "before" after init and then misuses the interface, which aborts.
+ * Prints OK and exits 0 on success. */
 #include <math.h>
 #include <stdint.h>
 #include <stdio.h>
@@ -82,6 +84,28 @@ int main(int argc, char** argv)
   {
     printf("%d failures\n", failures);
     return 1;
+  }
+  if(argc > 2)
+  {
+    /* one misuse after init, which must abort the process as the reference's
+     * death tests expect (quest_signed_distance_interface.cpp:245-335) */
+    double lo[3];
+    printf("before\n");
+    fflush(stdout);
+    switch(argv[2][0])
+    {
+    case '0': QUEST_signed_distance_set_closed_surface(true); break;
+    case '1': QUEST_signed_distance_set_dimension(3); break;
+    case '2': QUEST_signed_distance_set_verbose(true); break;
+    case '3': QUEST_signed_distance_set_execution_space(QUEST_SignedDistExec_CPU); break;
+    case '4': QUEST_signed_distance_get_mesh_bounds(NULL, lo); break;
+    case '5': QUEST_signed_distance_set_compute_signs(false); break;
+    case '6': QUEST_signed_distance_use_shared_memory(false); break;
+    case '7': QUEST_signed_distance_set_allocator(0); break;
+    default: break;
+    }
+    printf("after\n");
+    return 3;
   }
 
   const int N = 16;

@@ -129,3 +129,43 @@ def test_python_module_mirrors_the_reference_module():
     """)
     assert "before" in p.stdout and "after" not in p.stdout, p.stdout + p.stderr
     assert p.returncode == -signal.SIGABRT and "must be initialized" in p.stderr, p.stderr
+
+
+@pytest.fixture(scope="module")
+def mocked_c_caller(tmp_path_factory):
+    """tests/cpp/quest_check.c linked with libgsq.so and tests/cpp/quest_mock.cpp,
+    whose oracle-backed gsq_sdf_* functions take the place of the GPU query."""
+    from axom_gb300 import build
+    build.build()
+    d = tmp_path_factory.mktemp("quest_mock")
+    inc, lib_dir = ROOT / "include", ROOT / "axom_gb300"
+    subprocess.run(["gcc", "-std=c99", "-O1", f"-I{inc}", "-c", str(ROOT / "tests/cpp/quest_check.c"), "-o",
+                    str(d / "qc.o")], check=True)
+    subprocess.run(["g++", "-std=c++17", "-O1", "-ffp-contract=off", "-fopenmp", f"-I{inc}", "-c",
+                    str(ROOT / "tests/cpp/quest_mock.cpp"), "-o", str(d / "qm.o")], check=True)
+    exe = d / "quest_mocked"
+    subprocess.run(["g++", "-rdynamic", "-fopenmp", str(d / "qc.o"), str(d / "qm.o"), f"-L{lib_dir}", "-lgsq", "-lm",
+                    f"-Wl,-rpath,{lib_dir}", "-o", str(exe)], check=True)
+    return exe
+
+
+def test_c_caller_known_answers_on_the_oracle(mocked_c_caller, tmp_path):
+    """The interface's logic as built into libgsq.so, over the oracle: the
+    reference's plane known answers to 4 ulp, closest points and normals, the
+    nodes' bounds, a refused second init, finalize, a blank-padded Fortran name
+    and an unsigned re-init."""
+    p = subprocess.run([str(mocked_c_caller), str(tmp_path / "plane.stl")], capture_output=True, text=True,
+                       timeout=300)
+    assert p.returncode == 0 and "OK" in p.stdout, p.stdout + p.stderr
+
+
+@pytest.mark.parametrize("case,message", [("0", "already initialized"), ("1", "already initialized"),
+                                          ("2", "already initialized"), ("3", "already initialized"),
+                                          ("4", "buffer is null"), ("5", "already initialized"),
+                                          ("6", "already initialized"), ("7", "already initialized")])
+def test_misuse_after_init_aborts_on_the_oracle(mocked_c_caller, tmp_path, case, message):
+    p = subprocess.run([str(mocked_c_caller), str(tmp_path / "plane.stl"), case], capture_output=True, text=True,
+                       timeout=300)
+    assert "before" in p.stdout and "after" not in p.stdout, p.stdout + p.stderr
+    assert p.returncode == -signal.SIGABRT, (p.returncode, p.stderr)
+    assert message in p.stderr, p.stderr
