@@ -115,3 +115,24 @@ def test_callers_compile_and_link(lib, tmp_path):
                                  f"-L{lib_dir}", "-lgsq", "-lm", f"-Wl,-rpath,{lib_dir}", "-o", str(exe)],
                            capture_output=True, text=True)
         assert p.returncode == 0, p.stderr
+
+
+def test_cpp_shim_known_answers_on_the_oracle(lib, tmp_path):
+    """tests/cpp/shim_check.cpp (the reference's BVH, plane, STL, quest
+    interface and closest-point known answers through include/gsq.hpp) with
+    the GPU entry points taken over by the oracle-backed double
+    (tests/cpp/oracle_double.cpp): the shim's host logic on a machine without
+    a GPU.  The GPU suite runs the same program on the GPU entry points."""
+    import subprocess
+    inc, lib_dir = ROOT / "include", ROOT / "axom_gb300"
+    objs = []
+    for src, flags in (("shim_check.cpp", []), ("oracle_double.cpp", ["-ffp-contract=off", "-fopenmp"])):
+        obj = tmp_path / (src.split(".")[0] + ".o")
+        subprocess.run(["g++", "-std=c++17", "-O1", *flags, f"-I{inc}", "-c", str(ROOT / "tests/cpp" / src), "-o",
+                        str(obj)], check=True)
+        objs.append(str(obj))
+    exe = tmp_path / "shim_on_oracle"
+    subprocess.run(["g++", "-rdynamic", "-fopenmp", *objs, f"-L{lib_dir}", "-lgsq", f"-Wl,-rpath,{lib_dir}", "-o",
+                    str(exe)], check=True)
+    p = subprocess.run([str(exe)], capture_output=True, text=True, timeout=300, cwd=tmp_path)
+    assert p.returncode == 0 and "OK" in p.stdout, p.stdout + p.stderr

@@ -134,7 +134,7 @@ def test_python_module_mirrors_the_reference_module():
 
 @pytest.fixture(scope="module")
 def mocked_c_caller(tmp_path_factory):
-    """tests/cpp/quest_check.c linked with libgsq.so and tests/cpp/quest_mock.cpp,
+    """tests/cpp/quest_check.c linked with libgsq.so and tests/cpp/oracle_double.cpp,
     whose oracle-backed gsq_sdf_* functions take the place of the GPU query."""
     from axom_gb300 import build
     build.build()
@@ -143,7 +143,7 @@ def mocked_c_caller(tmp_path_factory):
     subprocess.run(["gcc", "-std=c99", "-O1", f"-I{inc}", "-c", str(ROOT / "tests/cpp/quest_check.c"), "-o",
                     str(d / "qc.o")], check=True)
     subprocess.run(["g++", "-std=c++17", "-O1", "-ffp-contract=off", "-fopenmp", f"-I{inc}", "-c",
-                    str(ROOT / "tests/cpp/quest_mock.cpp"), "-o", str(d / "qm.o")], check=True)
+                    str(ROOT / "tests/cpp/oracle_double.cpp"), "-o", str(d / "qm.o")], check=True)
     exe = d / "quest_mocked"
     subprocess.run(["g++", "-rdynamic", "-fopenmp", str(d / "qc.o"), str(d / "qm.o"), f"-L{lib_dir}", "-lgsq", "-lm",
                     f"-Wl,-rpath,{lib_dir}", "-o", str(exe)], check=True)
@@ -177,9 +177,9 @@ def test_python_module_on_the_oracle(tmp_path):
     the three evaluate forms, the result tuple of the second form, the array
     form and the bounds on the reference's open plane."""
     inc = ROOT / "include"
-    mock = tmp_path / "libquest_mock.so"
+    mock = tmp_path / "liboracle_double.so"
     subprocess.run(["g++", "-std=c++17", "-O1", "-ffp-contract=off", "-fopenmp", "-fPIC", "-shared", f"-I{inc}",
-                    str(ROOT / "tests/cpp/quest_mock.cpp"), "-o", str(mock)], check=True)
+                    str(ROOT / "tests/cpp/oracle_double.cpp"), "-o", str(mock)], check=True)
     stl = tmp_path / "plane.stl"
     stl.write_text("solid p\n" + "".join(
         f" facet normal 0 0 1\n  outer loop\n   vertex {a[0]} {a[1]} 0\n   vertex {b[0]} {b[1]} 0\n"
