@@ -3,7 +3,8 @@
 // (gsq_bvh_create / build / bounds / find_* / destroy and the scale and
 // tolerance setters), the signed distance (gsq_sdf_opts_init, gsq_sdf_create,
 // gsq_sdf_eval, gsq_sdf_mesh_bounds, gsq_sdf_destroy) and the closest object
-// point (gsq_cpq_create / query / destroy).  Linked into an executable with
+// point (gsq_cpq_create / query / destroy), and the option and timer queries
+// of the host mirrors.  Linked into an executable with
 // -rdynamic, or preloaded, these definitions take the place of libgsq.so's own,
 // so the host code above them (the quest interface in libgsq.so, the C++ shim
 // include/gsq.hpp, the Python modules) runs on a machine without a GPU, over
@@ -194,6 +195,45 @@ int gsq_cpq_query(const gsq_cpq* h, const double* points, int32_t m, double sq_t
 {
   if(!h || m < 0) return GSQ_ERR_INVALID;
   orc_cp_query(const_cast<gsq_cpq*>(h), points, m, sq_threshold, idx, dom, pos, dist, 1);
+  return GSQ_OK;
+}
+
+// ---- options and timers the host mirrors query (no GPU work: zero time,
+// no audit counters) -------------------------------------------------------
+int gsq_sdf_set_opts(gsq_sdf* h, const gsq_sdf_opts* o) { return (h && o) ? GSQ_OK : GSQ_ERR_INVALID; }
+
+int gsq_sdf_last_eval_ms(const gsq_sdf* h, float* ms)
+{
+  if(!h || !ms) return GSQ_ERR_INVALID;
+  *ms = 0.f;
+  return GSQ_OK;
+}
+
+int gsq_sdf_mixed_stats(const gsq_sdf* h, int64_t* c)
+{
+  if(!h || !c) return GSQ_ERR_INVALID;
+  for(int k = 0; k < 4; ++k) c[k] = 0;
+  return GSQ_OK;
+}
+
+int gsq_bvh_num_leaves(const gsq_bvh* b, int32_t* n)
+{
+  if(!b || !b->tree || !n) return GSQ_ERR_INVALID;
+  *n = orc_bvh_size(b->tree);
+  return GSQ_OK;
+}
+
+int gsq_bvh_last_build_ms(const gsq_bvh* b, float* ms)
+{
+  if(!b || !ms) return GSQ_ERR_INVALID;
+  *ms = 0.f;
+  return GSQ_OK;
+}
+
+int gsq_cpq_last_ms(const gsq_cpq* h, float* ms)
+{
+  if(!h || !ms) return GSQ_ERR_INVALID;
+  *ms = 0.f;
   return GSQ_OK;
 }
 
