@@ -1,10 +1,13 @@
-// The FP32 leaf certificate of the mixed signed distance: the per-query
-// context, the point-triangle distance evaluated in FP32, its error bounds, the
-// test that the reference's fuzzy region tests take their exact outcomes, and
-// the per-triangle error terms stored in the FP32 leaf records.
+// The FP32 certificates of the mixed signed distance: the per-query context;
+// for the leaves, the point-triangle distance evaluated in FP32, its error
+// bounds, the test that the reference's fuzzy region tests take their exact
+// outcomes, and the per-triangle error terms stored in the FP32 leaf records;
+// for the nodes, the outward-rounded child boxes of the FP32 node records, the
+// box test and the child order.
 //
-// The functions compile for the device (the query kernels) and for the host (a
-// checker in the tests compares them with the oracle's FP64 closest point).
+// The functions compile for the device (the query kernels) and for the host
+// (checkers in the tests compare them with the oracle's FP64 closest point and
+// node visit).
 // fp:: names the roundings: on the device they are the CUDA intrinsics; on
 // the host round-to-nearest operations are the same IEEE operations, and a
 // directed rounding is the nearest result moved one ulp outward, never tighter
