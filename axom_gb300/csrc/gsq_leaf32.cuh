@@ -279,6 +279,12 @@ GSQ_HD void tri_error_terms(const double* A, const double* B, const double* C, f
   const double mt = fmax(fmax(fmax(fabs(A[0]), fabs(A[1])), fmax(fabs(A[2]), fabs(B[0]))),
                          fmax(fmax(fabs(B[1]), fabs(B[2])), fmax(fmax(fabs(C[0]), fabs(C[1])), fabs(C[2]))));
   if(!(2.06e-12 * kappa / L <= 0x1p-22 * mt)) ec = INFINITY;
+  // The conditioning factor is the FP64 triangle's; the FP32 one has its
+  // vertices moved by up to d = sqrt(3) 2^-24 mt, which changes the cross
+  // product by about 4 d L, i.e. its altitude h = |n| / L by 4 d.  Slivers
+  // narrower than 64 d (their rounded form can be far thinner, even flipped)
+  // get an infinite factor too: never skipped, bounds from FP64.
+  if(!(64.0 * 1.7320508075688774 * 0x1p-24 * mt * L <= nn)) ec = INFINITY;
   lt = fp::f_ru(L * 1.0001);
   if(fz)
   {

@@ -30,3 +30,14 @@ def test_leaf_certificate_bounds(leaf_check, mode):
     assert r.returncode == 0, r.stdout + r.stderr
     counts = r.stdout.split("|")[0].split()
     assert int(counts[counts.index("skipped") + 1]) > 0 and int(counts[counts.index("kept") + 1]) > 0, r.stdout
+
+
+def test_leaf_certificate_sliver_thinner_than_rounding(leaf_check):
+    """Seed 901 of mode 1 draws a quad's sliver 6.7e-7 wide at coordinates
+    near 44, whose FP32 vertices move by 4.5e-6: the rounded triangle is far
+    thinner than the FP64 one, and a conditioning factor taken from the FP64
+    triangle let the certificate skip it at an FP64 distance of 5.7e-7.
+    Triangles narrower than 64 times their vertices' rounding are never
+    skipped now."""
+    r = subprocess.run([str(leaf_check), "5000000", "901", "1"], capture_output=True, text=True)
+    assert r.returncode == 0, r.stdout + r.stderr
