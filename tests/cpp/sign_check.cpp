@@ -10,7 +10,9 @@
 // outward, never tighter than the device's, and the reciprocal square root and
 // arccosine are evaluated in FP64 and rounded.  Whenever the certificate gives
 // a sign it must be the FP64 test's.
-// Usage: sign_check <cases> <seed>; prints counts, exits 1 on a violation.
+// Usage: sign_check <cases> <seed> [mode]; mode 1 places the geometry at
+// coordinates up to 1e3 (default: up to 2).  Prints counts, exits 1 on a
+// violation.
 #include <cmath>
 #include <cstdio>
 #include <cstdlib>
@@ -70,6 +72,7 @@ int main(int argc, char** argv)
 {
   const long long cases = argc > 1 ? std::atoll(argv[1]) : 100000;
   const unsigned seed = argc > 2 ? (unsigned)std::atoi(argv[2]) : 1;
+  const int mode = argc > 3 ? std::atoi(argv[3]) : 0;
   std::mt19937_64 rng(seed);
   std::uniform_real_distribution<double> U01(0.0, 1.0);
   std::normal_distribution<double> G(0.0, 1.0);
@@ -82,7 +85,7 @@ int main(int argc, char** argv)
   for(long long c = 0; c < cases; ++c)
   {
     const int kind = (int)(c % 3);  // 0 face, 1 shared vertex, 2 shared edge
-    const double R = unif(0.0, 2.0);
+    const double R = mode == 1 ? std::pow(10.0, unif(0, 3)) : unif(0.0, 2.0);
     double V[3], e1[3], e2[3], e3[3], g[3];
     for(int d = 0; d < 3; ++d) V[d] = unif(-R, R), e3[d] = G(rng), g[d] = G(rng);
     normalize(e3);
