@@ -11,8 +11,9 @@
 //   kept (true)      =>  l2 <= FP64 squared distance <= h2 and
 //                        |cpf - FP64 closest point| <= rad.
 // Usage: leaf_check <cases> <seed> [mode]; mode 0 mixed sizes, 1 coordinates
-// up to 1e3, 2 triangles of 1e-6..1e-4, 3 points up to 1e2 away.  Prints
-// counts and exits 1 on a violation.
+// up to 1e3, 2 triangles of 1e-6..1e-4, 3 points up to 1e2 away, 4 triangles
+// of 1e-6..1e-4 at coordinates up to 1e3.  Prints counts and exits 1 on a
+// violation.
 #include <algorithm>
 #include <cmath>
 #include <cstdio>
@@ -93,8 +94,8 @@ int main(int argc, char** argv)
     // a triangle: small (fine meshes), unit-sized, or a sliver, at a random place
     const int kind = (int)(k % 4);
     double scale = kind == 2 ? unif(0.1, 1.0) : std::pow(10.0, unif(-3.5, -1.5));
-    if(mode == 2) scale = std::pow(10.0, unif(-6, -4));
-    const double R = mode == 1 ? std::pow(10.0, unif(0, 3)) : unif(0.0, 2.0);
+    if(mode == 2 || mode == 4) scale = std::pow(10.0, unif(-6, -4));
+    const double R = (mode == 1 || mode == 4) ? std::pow(10.0, unif(0, 3)) : unif(0.0, 2.0);
     double A[3], B[3], C[3];
     for(int d = 0; d < 3; ++d) A[d] = unif(-R, R);
     for(int d = 0; d < 3; ++d) B[d] = A[d] + scale * unif(-1, 1);

@@ -6,8 +6,8 @@ comparisons included) and an exact long-double distance: a skipped
 triangle's FP64 distance exceeds the threshold, a kept triangle's FP64 squared
 distance lies in [l2, h2], and its FP64 closest point lies within rad of the
 estimate.  Random triangles of mixed sizes, slivers (kappa up to 2^20),
-coordinates up to 1e3, tiny triangles and distant points; quads' triangles
-too."""
+coordinates up to 1e3, tiny triangles (also at coordinates up to 1e3) and
+distant points; quads' triangles too."""
 import subprocess
 from pathlib import Path
 
@@ -24,7 +24,7 @@ def leaf_check(tmp_path_factory):
     return exe
 
 
-@pytest.mark.parametrize("mode", [0, 1, 2, 3])
+@pytest.mark.parametrize("mode", [0, 1, 2, 3, 4])
 def test_leaf_certificate_bounds(leaf_check, mode):
     r = subprocess.run([str(leaf_check), "1000000", str(31 + mode), str(mode)], capture_output=True, text=True)
     assert r.returncode == 0, r.stdout + r.stderr
