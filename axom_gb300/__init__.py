@@ -94,6 +94,7 @@ SIGNATURES = [
     ("gsq_ray_normalize", C.c_int, [_dp, C.c_int32, _dp]),
     ("gsq_bvh_export", C.c_int, [_vp, _dp, _ip, _ip, _up]),
     ("gsq_bvh_last_build_ms", C.c_int, [_vp, C.POINTER(C.c_float)]),
+    ("gsq_bvh_last_find_ms", C.c_int, [_vp, C.POINTER(C.c_float)]),
     ("gsq_sdf_opts_init", C.c_int, [C.POINTER(SdfOpts)]),
     ("gsq_sdf_create", C.c_int, [C.POINTER(_vp), _vp, _vp, _vp, C.c_int32, _vp, C.c_int32, C.c_int32, C.c_int32,
                                  C.c_int32, C.POINTER(SdfOpts), _vp]),
@@ -277,6 +278,12 @@ class BVH:
     def last_build_ms(self) -> float:
         v = C.c_float()
         _check(self._lib.gsq_bvh_last_build_ms(self._h, C.byref(v)))
+        return v.value
+
+    def last_find_ms(self) -> float:
+        """Device time of the last find's traversal passes and scan."""
+        v = C.c_float()
+        _check(self._lib.gsq_bvh_last_find_ms(self._h, C.byref(v)))
         return v.value
 
     def get_view(self) -> BvhView:

@@ -511,6 +511,7 @@ struct gsq_bvh
   gsq::BvhDev dev;
   bool built = false;
   float build_ms = 0.f;
+  mutable float find_ms = 0.f;  // device time of the last find's two passes and scan
   int* d_err = nullptr;
 };
 
@@ -547,6 +548,9 @@ int find_impl(const gsq_bvh* h, const double* a, const double* b, int32_t m, int
   QueryArgs qa {static_cast<const double*>(qa_buf.dev), static_cast<const double*>(qb_buf.dev), h->tol};
   int* d_cnt = static_cast<int*>(cnt_buf.dev);
   int* d_off = static_cast<int*>(off_buf.dev);
+  Events ev;
+  GSQ_CUDA_TRY(ev.create());
+  cudaEventRecord(ev.e[0], s);
   if(m > 0)
   {
     count_launch();
@@ -555,6 +559,7 @@ int find_impl(const gsq_bvh* h, const double* a, const double* b, int32_t m, int
   }
   rc = exclusive_scan(d_cnt, d_off, m, tot.as<long long>(), s);
   if(rc) return rc;
+  cudaEventRecord(ev.e[1], s);
   long long total = 0;
   GSQ_CUDA_TRY(cudaMemcpyAsync(&total, tot.p, sizeof(long long), cudaMemcpyDeviceToHost, s));
   GSQ_CUDA_TRY(cudaStreamSynchronize(s));
@@ -563,12 +568,14 @@ int find_impl(const gsq_bvh* h, const double* a, const double* b, int32_t m, int
   if(total > INT_MAX) return fail(GSQ_ERR_INVALID, "more than 2^31-1 candidates");
   int* d_cand = nullptr;
   GSQ_CUDA_TRY(cudaMalloc(&d_cand, sizeof(int) * (size_t)std::max<long long>(total, 1)));
+  cudaEventRecord(ev.e[2], s);
   if(m > 0)
   {
     count_launch();
     k_find_pass2<KIND><<<grid_for(m, FIND_THREADS), FIND_THREADS, 0, s>>>(h->dev.nodes, h->dev.perm, qa, m, d_cnt,
                                                                           d_off, keep.as<int>(), d_cand);
   }
+  cudaEventRecord(ev.e[3], s);
   cudaError_t e = cudaGetLastError();
   if(e == cudaSuccess) e = off_buf.flush(s);
   if(e == cudaSuccess) e = cnt_buf.flush(s);
@@ -601,6 +608,10 @@ int find_impl(const gsq_bvh* h, const double* a, const double* b, int32_t m, int
     return cuda_fail(e, "find pass 2");
   }
   if(total_out) *total_out = total;
+  float t01 = 0.f, t23 = 0.f;
+  cudaEventElapsedTime(&t01, ev.e[0], ev.e[1]);
+  cudaEventElapsedTime(&t23, ev.e[2], ev.e[3]);
+  h->find_ms = t01 + t23;
   return GSQ_OK;
 }
 }  // namespace
@@ -708,6 +719,13 @@ int gsq_bvh_last_build_ms(const gsq_bvh* h, float* ms)
 {
   if(!h || !ms) return fail(GSQ_ERR_INVALID, "null argument");
   *ms = h->build_ms;
+  return GSQ_OK;
+}
+
+int gsq_bvh_last_find_ms(const gsq_bvh* h, float* ms)
+{
+  if(!h || !ms) return fail(GSQ_ERR_INVALID, "null argument");
+  *ms = h->find_ms;
   return GSQ_OK;
 }
 

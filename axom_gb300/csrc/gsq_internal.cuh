@@ -69,6 +69,29 @@ struct Scratch
   }
 };
 
+// Four CUDA events, destroyed with the object (timing of one call).
+struct Events
+{
+  cudaEvent_t e[4] = {nullptr, nullptr, nullptr, nullptr};
+  Events() = default;
+  Events(const Events&) = delete;
+  Events& operator=(const Events&) = delete;
+  ~Events()
+  {
+    for(auto& x : e)
+      if(x) cudaEventDestroy(x);
+  }
+  cudaError_t create()
+  {
+    for(auto& x : e)
+    {
+      const cudaError_t r = cudaEventCreate(&x);
+      if(r != cudaSuccess) return r;
+    }
+    return cudaSuccess;
+  }
+};
+
 // Device buffer that is either the caller's device pointer or a staged copy
 // of the caller's host array.
 struct InBuf

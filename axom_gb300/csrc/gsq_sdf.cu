@@ -484,14 +484,16 @@ int gsq_sdf_eval(const gsq_sdf* hc, const double* qx, const double* qy, const do
 // Allocation-free evaluation
 // =============================================================================
 // Some callers cannot allocate device memory while they evaluate distances:
-// code that owns all device memory through its own pool allocator and forbids
-// other allocations, code whose evaluation runs inside a CUDA stream capture
-// (where cudaMalloc is not allowed), and time-critical loops where the
-// device-wide synchronisation of cudaMalloc/cudaFree is unacceptable.  For them
-// gsq_sdf_eval_noalloc takes the query points and the output in device memory
-// and keeps its only scratch -- the Morton-order sort of the queries -- in the
-// fixed array below, which every GPU that loads this library holds until the
-// process exits.
+// applications whose own pool allocator owns all device memory and forbids
+// allocations behind its back, and loops running beside other streams that
+// must not be stalled by the implicit device-wide synchronisation of
+// cudaMalloc/cudaFree (this call waits only for its own stream, to read the
+// device error flag).  For them gsq_sdf_eval_noalloc takes the query points
+// and the output in device memory and keeps its only scratch -- the
+// Morton-order sort of the queries -- in the fixed array below, which every
+// GPU that loads this library holds until the process exits.  The array's
+// address is looked up once per device and kept; a cudaDeviceReset, which
+// also invalidates every handle, is not supported after the first call.
 namespace
 {
 constexpr int NOALLOC_MAX = GSQ_NOALLOC_MAX_QUERIES;
@@ -541,6 +543,11 @@ int gsq_sdf_eval_noalloc(const gsq_sdf* hc, const double* qx, const double* qy, 
   if(!qx || !qy || !qz || !out) return fail(GSQ_ERR_INVALID, "null query or output array");
   if(!is_device_ptr(qx) || !is_device_ptr(qy) || !is_device_ptr(qz) || !is_device_ptr(out))
     return fail(GSQ_ERR_INVALID, "gsq_sdf_eval_noalloc: queries and output must be device memory");
+  int dev = 0;
+  GSQ_CUDA_TRY(cudaGetDevice(&dev));
+  if(dev != h->device)
+    return fail(GSQ_ERR_INVALID, "gsq_sdf_eval_noalloc: the current device (" + std::to_string(dev) +
+                                     ") is not the handle's device (" + std::to_string(h->device) + ")");
   cudaStream_t s = static_cast<cudaStream_t>(stream);
   void* base = nullptr;
   int rc = noalloc_scratch(&base);

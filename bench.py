@@ -39,11 +39,18 @@ MESH_SEED = 1234
 QUERIES = 1 << 24
 FALLBACK_HBM_GBS = 6800.0
 BATCH_MESHES = 512
-# DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) per point of one
-# k_sdf_mixed launch, measured by ncu on 1,048,576 uniform points of the same
-# mesh (1.432 GB read + 0.373 GB written); the bench scales it by its point count.
-MIXED_DRAM_BYTES_PER_POINT = (1.432073e9 + 0.373072e9) / 1048576
+# Per point of one k_sdf_mixed launch, from the ncu capture summarised in
+# profiles/k_sdf_mixed_level8_uniform_1M.md (1,048,576 uniform points of the
+# same mesh): DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) and L2
+# bytes (lts__t_sectors.sum x 32); the bench scales them by its point count.
+MIXED_DRAM_BYTES_PER_POINT = (1.471348e9 + 0.393579e9) / 1048576
+MIXED_L2_BYTES_PER_POINT = 2993155879 * 32 / 1048576
 BATCH_SEED = 5
+# The 100,000-box workload: boxes from seed 1, query boxes from seed 2.
+C1_BOXES = 100_000
+# Algorithmic bytes of one build per box: boxes read (48), codes and
+# permutation through 4 LSD passes (2 x 8 each), tree links (12), refit (2 x 48).
+BUILD_BYTES_PER_BOX = 48 + 4 * 2 * 8 + 12 + 2 * 48
 
 
 def parse():
@@ -126,6 +133,79 @@ def algorithmic_bytes_per_query(port, v, f, q_sample, threads):
     return 32.0 + 104.0 * nb.mean() / 2.0 + 88.0 * nl.mean(), float(nb.mean()), float(nl.mean())
 
 
+def median_time(fn, reps=3):
+    ts = []
+    for _ in range(reps):
+        t0 = time.perf_counter()
+        fn()
+        ts.append(time.perf_counter() - t0)
+    return statistics.median(ts)
+
+
+def config1_leg(args, G, torch, port, threads):
+    """The 100,000-box workload (BVH::initialize over 100,000 boxes, then
+    findBoundingBoxes for 100,000 query boxes): device build and find times
+    with their rooflines, the whole call with host buffers, the CSR against
+    the oracle, and the oracle port's 1-thread and all-thread times."""
+    from axom_gb300 import workloads as W
+    boxes = W.random_boxes(C1_BOXES, 1)
+    q = W.random_boxes(C1_BOXES, 2)
+    bd = torch.from_numpy(boxes).cuda()
+    qd = torch.from_numpy(q).cuda()
+    bvh = G.BVH()
+    build_ms, find_ms, find_call_ms = [], [], []
+    for i in range(args.warmup + args.steps):
+        bvh.initialize(bd)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        res = bvh.find_bounding_boxes(qd)
+        torch.cuda.synchronize()
+        if i >= args.warmup:
+            build_ms.append(bvh.last_build_ms())
+            find_ms.append(bvh.last_find_ms())
+            find_call_ms.append((time.perf_counter() - t0) * 1000.0)
+    off, cnt, cand = (r.cpu().numpy() for r in res)
+    # end to end: host boxes in, host CSR out, copies inside
+    e2e = []
+    for i in range(args.warmup + args.steps):
+        t0 = time.perf_counter()
+        hb = G.BVH(boxes)
+        hres = hb.find_bounding_boxes(q)
+        if i >= args.warmup:
+            e2e.append((time.perf_counter() - t0) * 1000.0)
+    hp = port.bvh(boxes)
+    want = port.find_boxes(hp, q)
+    equal = all(np.array_equal(np.asarray(a), b) for a, b in zip((off, cnt, cand), want)) and \
+        all(np.array_equal(np.asarray(a), b) for a, b in zip(hres, want))
+    nb = port.find_boxes_counts(hp, q)
+    bq = 48.0 + 104.0 * nb.mean() / 2.0 + 4.0 * (cand.size / C1_BOXES + 2.0)
+    hbm, kind = peaks()
+    bms, fms = statistics.median(build_ms), statistics.median(find_ms)
+    build_gbs = BUILD_BYTES_PER_BOX * C1_BOXES / (bms / 1000.0) / 1e9
+    find_gbs = bq * C1_BOXES / (fms / 1000.0) / 1e9
+    cpu_build_1 = median_time(lambda: port.bvh(boxes))
+    cpu_find_1 = median_time(lambda: port.find_boxes(hp, q))
+    cpu_find_n = median_time(lambda: port.find_boxes_mt(hp, q, threads))
+    return {
+        "workload": f"{C1_BOXES} boxes (seed 1) and {C1_BOXES} query boxes (seed 2): centres U[0,1]^3, "
+                    "sides log-uniform in [1e-3, 1e-2]; scale 1.000123",
+        "build_ms": bms, "find_ms": fms, "find_call_ms": statistics.median(find_call_ms),
+        "candidates": int(cand.size), "box_tests_per_query": float(nb.mean()),
+        "e2e_ms": statistics.median(e2e), "e2e_note": "host boxes in, host CSR out: build + find calls, copies inside",
+        "oracle_equal": bool(equal),
+        "roofline_build": {"bound": "hbm", "achieved": build_gbs, "peak": hbm, "unit": "GB/s",
+                           "frac": build_gbs / hbm, "peak_kind": kind,
+                           "algorithmic_bytes_per_box": BUILD_BYTES_PER_BOX},
+        "roofline_find": {"bound": "hbm", "achieved": find_gbs, "peak": hbm, "unit": "GB/s",
+                          "frac": find_gbs / hbm, "peak_kind": kind, "algorithmic_bytes_per_query": bq},
+        "cpu_baseline": {"kind": "port", "build_ms_1_thread": 1000.0 * cpu_build_1,
+                         "find_ms_1_thread": 1000.0 * cpu_find_1, "find_ms_all_threads": 1000.0 * cpu_find_n,
+                         "cores": threads,
+                         "sample": "the whole workload, median of 3; the build is serial as the reference's SEQ "
+                                   "path is; the threaded find splits the queries into contiguous ranges"},
+    }
+
+
 def cpu_baseline(port, v, f, q, seconds, threads):
     """The oracle port on the host cores, on a bounded stratified sample."""
     h = port.sdf(v[:, 0], v[:, 1], v[:, 2], f)
@@ -138,9 +218,24 @@ def cpu_baseline(port, v, f, q, seconds, threads):
     t0 = time.perf_counter()
     port.sdf_eval(h, sample, threads=threads)
     dt = time.perf_counter() - t0
+    # one core, on a smaller stratified sample (about a fifth of the time above)
+    n1 = int(min(q.shape[0], max(500, rate / threads * seconds / 5)))
+    s1 = q[np.linspace(0, q.shape[0] - 1, n1).astype(np.int64)]
+    t0 = time.perf_counter()
+    port.sdf_eval(h, s1, threads=1)
+    dt1 = time.perf_counter() - t0
+    # the SignedDistance constructor (mesh box, cell boxes, BVH::initialize) and
+    # BVH::initialize alone over the triangle boxes, one core
+    sdf_ctor = median_time(lambda: port.sdf(v[:, 0], v[:, 1], v[:, 2], f))
+    tri = v[f]
+    tboxes = np.concatenate([tri.min(1), tri.max(1)], 1)
+    bvh_init = median_time(lambda: port.bvh(tboxes))
     return {"value": n / dt, "unit": UNIT, "cores": threads, "kind": "port",
             "sample": f"{n} stratified points of the {q.shape[0]} (every {q.shape[0] // n}th), "
-                      f"{dt:.1f} s on {threads} host threads"}
+                      f"{dt:.1f} s on {threads} host threads",
+            "one_core": {"value": n1 / dt1, "unit": UNIT, "sample": f"{n1} stratified points, {dt1:.1f} s"},
+            "sdf_ctor_ms_1_thread": 1000.0 * sdf_ctor, "bvh_init_ms_1_thread": 1000.0 * bvh_init,
+            "bvh_init_boxes": int(f.shape[0])}
 
 
 def dist_setup():
@@ -246,9 +341,12 @@ def batched_leg(args, G, torch, lib, threads):
         v, f = meshes[k]
         ref = G.SignedDistance(v, f).compute_distances(pts[k][:20000])
         exact &= bool(np.array_equal(ref.view(np.int64), parts[k][:20000].view(np.int64)))
-    # CPU estimate: the port builds and queries a sample of meshes on all host cores
+    # CPU baseline, timed on a sample: the port builds 16 of the meshes (evenly
+    # spaced, 1 thread, as the reference's SEQ build) and evaluates a stratified
+    # sample of each one's points (all host threads); the rate is the sample's
+    # points over the sample's build + query time
     port = oracle.Port()
-    sample_meshes = np.linspace(0, len(meshes) - 1, 8).astype(int)
+    sample_meshes = np.linspace(0, len(meshes) - 1, 16).astype(int)
     cpu_build_s, cpu_tris, cpu_q_s, cpu_q = 0.0, 0, 0.0, 0
     for k in sample_meshes:
         v, f = meshes[k]
@@ -256,12 +354,12 @@ def batched_leg(args, G, torch, lib, threads):
         h = port.sdf(v[:, 0], v[:, 1], v[:, 2], f)
         cpu_build_s += time.perf_counter() - t0
         cpu_tris += f.shape[0]
-        qs = pts[k][: min(pts[k].shape[0], 4000)]
+        pk = pts[k]
+        qs = pk[np.linspace(0, pk.shape[0] - 1, min(pk.shape[0], 20000)).astype(np.int64)]
         t0 = time.perf_counter()
         port.sdf_eval(h, qs, threads=threads)
         cpu_q_s += time.perf_counter() - t0
         cpu_q += qs.shape[0]
-    est_step_s = tris * cpu_build_s / cpu_tris + m * cpu_q_s / cpu_q
     return {
         "workload": f"batched form: {len(meshes)} icospheres (levels 2-6, {tris} triangles), {m} points "
                     f"(log-uniform 1k-1M per mesh); a step rebuilds every tree and evaluates every point",
@@ -272,10 +370,11 @@ def batched_leg(args, G, torch, lib, threads):
         "e2e": {"value": m / (e2e_ms / 1000.0), "unit": UNIT, "ms_per_step": e2e_ms,
                 "h2d_bytes_per_step": 24 * m + 24 * int(allv.shape[0]), "d2h_bytes_per_step": 8 * m},
         "spot_check_bit_exact": exact,
-        "cpu_baseline": {"value": m / est_step_s, "unit": UNIT, "cores": threads, "kind": "port",
-                         "sample": f"estimated: port build of {len(sample_meshes)} meshes ({cpu_tris} triangles, "
-                                   f"1 thread) and {cpu_q} of their points ({threads} threads), scaled to the "
-                                   f"batch's {tris} triangles and {m} points"},
+        "cpu_baseline": {"value": cpu_q / (cpu_build_s + cpu_q_s), "unit": UNIT, "cores": threads, "kind": "port",
+                         "build_s": cpu_build_s, "query_s": cpu_q_s,
+                         "sample": f"timed: port build of {len(sample_meshes)} of the meshes ({cpu_tris} triangles, "
+                                   f"1 thread) and {cpu_q} stratified points of those meshes ({threads} threads); "
+                                   f"rate = sample points / (build + query seconds)"},
     }
 
 
@@ -453,9 +552,13 @@ def run_gsq(args, world, rank, local):
     other = G.PRECISION_FP64 if prec == G.PRECISION_MIXED else None
     fp64 = None
     if other is not None:
+        out_mixed = out.clone()
         ms64, kms64, _ = run_steps(other, max(1, min(args.steps, 3)), 1)
         fp64 = {"value": world * m / (ms64 / 1000.0), "ms_per_step": ms64, "kernel_ms": kms64,
-                "speedup_mixed_over_fp64": ms64 / ms}
+                "speedup_mixed_over_fp64": ms64 / ms,
+                "mixed_bit_identical": bool(torch.equal(out_mixed.view(torch.int64), out.view(torch.int64))),
+                "sign_mismatches": int((torch.signbit(out_mixed) != torch.signbit(out)).sum().item())}
+        del out_mixed
         sd.set_precision(prec)
 
     # End to end through the public API with host buffers: pinned host points in,
@@ -490,7 +593,11 @@ def run_gsq(args, world, rank, local):
         "build_ms": {"value": statistics.median(build_ms), "boxes": int(f.shape[0]), "runs": len(build_ms)},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
                      "traffic": MIXED_DRAM_BYTES_PER_POINT * m if args.precision == "mixed" else None,
-                     "traffic_note": "ncu DRAM bytes per point on a 1,048,576-point launch, scaled to this launch",
+                     "traffic_note": "ncu DRAM bytes per point on a 1,048,576-point launch, scaled to this launch "
+                                     "(profiles/k_sdf_mixed_level8_uniform_1M.md)",
+                     "l2_bytes": MIXED_L2_BYTES_PER_POINT * m if args.precision == "mixed" else None,
+                     "l2_gbs": (MIXED_L2_BYTES_PER_POINT * m / (kernel_ms / 1000.0) / 1e9
+                                if args.precision == "mixed" else None),
                      "peak_kind": hbm_kind,
                      "kernel": "k_sdf_mixed" if args.precision == "mixed" else "k_sdf_fp64",
                      "kernel_ms": kernel_ms,
@@ -503,6 +610,7 @@ def run_gsq(args, world, rank, local):
     if world == 1 and not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline(port, v, f, q_host, args.cpu_seconds, threads)
     if world == 1 and args.forms:
+        line["config1"] = config1_leg(args, G, torch, port, threads)
         line["near_surface"] = near_surface_leg(args, G, torch, v, f)
         line["adjoint"] = adjoint_leg(args, G, torch)
         line["closest_point"] = closest_point_leg(args, G, torch, port, v, threads)

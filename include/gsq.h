@@ -149,6 +149,11 @@ int gsq_bvh_get_view(const gsq_bvh* bvh, gsq_bvh_view* view);
  * handle (CUDA events around the build's kernels). */
 int gsq_bvh_last_build_ms(const gsq_bvh* bvh, float* ms);
 
+/* Milliseconds of device time taken by the last find on this handle: its two
+ * traversal passes and the offsets scan (CUDA events on the call's stream;
+ * the host wait for the candidate count between them is not included). */
+int gsq_bvh_last_find_ms(const gsq_bvh* bvh, float* ms);
+
 /* ---- quest::SignedDistance --------------------------------------------- */
 
 typedef struct gsq_sdf_opts {
@@ -195,19 +200,24 @@ int gsq_sdf_eval(const gsq_sdf* sdf, const double* qx, const double* qy, const d
                  int32_t m, double* out, double* closest, double* normals, void* stream);
 
 /* Allocation-free evaluation, for callers that must not allocate device
- * memory while evaluating: code that owns all device memory through its own
- * pool, code evaluating inside a CUDA stream capture (where cudaMalloc is not
- * allowed), and latency-bound loops that cannot afford the device-wide
- * synchronisation of cudaMalloc/cudaFree.  No counterpart in the reference.
+ * memory while evaluating: applications whose own pool allocator owns all
+ * device memory, and loops beside other streams that must not be stalled by
+ * the implicit device-wide synchronisation of cudaMalloc/cudaFree.  No
+ * counterpart in the reference.
  *   - qx, qy, qz (with `stride`, as gsq_sdf_eval) and out (m doubles) must be
  *     device memory; no closest points or normals.
+ *   - Runs on the handle's device, which must be the current device
+ *     (else GSQ_ERR_INVALID).  Returns after its stream has finished (it
+ *     reads the device error flag), as gsq_sdf_eval does.
  *   - m <= GSQ_NOALLOC_MAX_QUERIES, else GSQ_ERR_INVALID and nothing runs.
  *   - Calls no cudaMalloc/cudaFree or allocating library routine.  The only
  *     scratch (the Morton-order sort of the points) is one fixed array of
  *     about 4.3 MB in the library's device image, which every GPU that loads
  *     the library holds until the process exits.
  *   - The first call on each device looks the array's device address up once
- *     (cudaGetSymbolAddress); make that first call before any stream capture.
+ *     (cudaGetSymbolAddress) and keeps it; make that first call before any
+ *     stream capture.  A cudaDeviceReset after it is not supported (it also
+ *     invalidates every handle).
  *   - Every call shares that one array: calls whose GPU work overlaps (other
  *     streams or host threads, on the same device) race and corrupt each
  *     other's results.  Serialise them.

@@ -27,7 +27,6 @@ HERE = Path(__file__).resolve().parent
 PORT_SRC = HERE / "gsq_oracle.cpp"
 PORT_LIB = HERE / "_build" / "libgsq_oracle.so"
 REF_LIB = HERE / "_ref" / "libaxom_ref.so"
-DEFAULT_REFERENCE = Path(os.environ.get("AXOM_REFERENCE_DIR", "/root/reference"))
 
 _dp = C.POINTER(C.c_double)
 _ip = C.POINTER(C.c_int)
@@ -45,12 +44,14 @@ def build_port(force: bool = False) -> Path:
     return PORT_LIB
 
 
-def build_reference(reference: Path = DEFAULT_REFERENCE) -> Path | None:
-    """Build the reference's own SEQ path when its sources are present."""
-    if not (reference / "src/axom/spin/BVH.hpp").exists():
-        return None
+def build_reference(reference: Path | None = None) -> Path | None:
+    """Build the reference's own SEQ path when its sources are present
+    (``reference`` defaults to the recipe's ``DEFAULT_REFERENCE``)."""
     import importlib
     br = importlib.import_module(__name__ + ".build_ref")
+    reference = Path(reference) if reference is not None else br.DEFAULT_REFERENCE
+    if not (reference / "src/axom/spin/BVH.hpp").exists():
+        return None
     return br.build(reference, os.cpu_count() or 4)
 
 
@@ -122,6 +123,15 @@ class _Lib:
     def find_points(self, h, p):
         p = _arr(p, np.float64).reshape(-1, 3)
         return self._csr(self.f("bvh_find_points"), h, p, p.shape[0], _p(p), p.shape[0])
+
+    def find_boxes_counts(self, h, q):
+        """Box-predicate calls of findBoundingBoxes' traversal, per query."""
+        q = _arr(q, np.float64).reshape(-1, 6)
+        nb = np.empty(q.shape[0], np.int32)
+        fn = self.f("bvh_find_boxes_counts")
+        fn.argtypes = [C.c_void_p, _dp, C.c_int, _ip]
+        fn(h.ptr, _p(q), q.shape[0], _p(nb))
+        return nb
 
     # ---- closest object point (DistributedClosestPoint's local query) -----
     def cp(self, pts, domains=None):
@@ -217,6 +227,22 @@ class Port(_Lib):
         h = self.lib.orc_sdf_create(_p(x), _p(y), _p(z), x.size, _p(cells), cells.size // npc, npc,
                                     int(watertight), int(compute_sign))
         return _Handle(self, h, "sdf_destroy")
+
+    def find_boxes_mt(self, h, q, threads):
+        """findBoundingBoxes over contiguous sub-ranges of the queries on
+        `threads` threads; the same CSR as find_boxes."""
+        q = _arr(q, np.float64).reshape(-1, 6)
+        fn = self.lib.orc_bvh_find_boxes_mt
+        fn.restype = C.c_longlong
+        fn.argtypes = [C.c_void_p, _dp, C.c_int, _ip, _ip, C.POINTER(_ip), C.c_int]
+        m = q.shape[0]
+        off = np.empty(m, np.int32)
+        cnt = np.empty(m, np.int32)
+        cp = _ip()
+        total = fn(h.ptr, _p(q), m, _p(off), _p(cnt), C.byref(cp), threads)
+        cand = np.ctypeslib.as_array(cp, shape=(max(total, 1),))[:total].copy() if total else np.empty(0, np.int32)
+        self.f("free")(cp)
+        return off, cnt, cand
 
     def normalize_rays(self, d):
         d = _arr(d, np.float64).reshape(-1, 3)

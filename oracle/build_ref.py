@@ -28,6 +28,10 @@ import sys
 from pathlib import Path
 
 HERE = Path(__file__).resolve().parent
+# Where the reference tree is mounted: AXOM_REFERENCE_DIR or --reference, else
+# the mount point of the container this recipe runs in (this file is the only
+# one that names it; the GPU host has no reference tree and never builds it).
+DEFAULT_REFERENCE = Path(os.environ.get("AXOM_REFERENCE_DIR") or "/root/reference")
 OUT = HERE / "_ref"
 GEN = OUT / "gen"
 OBJ = OUT / "obj"
@@ -166,7 +170,7 @@ def build(reference: Path, jobs: int) -> Path:
 
 def main() -> int:
     ap = argparse.ArgumentParser()
-    ap.add_argument("--reference", default="/root/reference")
+    ap.add_argument("--reference", default=str(DEFAULT_REFERENCE))
     ap.add_argument("-j", type=int, default=os.cpu_count() or 4)
     a = ap.parse_args()
     print(build(Path(a.reference), a.j))

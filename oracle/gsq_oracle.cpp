@@ -791,6 +791,53 @@ long long orc_bvh_find_boxes(void* h, const double* q, int m, int* offsets, int*
     offsets, counts, cands);
 }
 
+// findBoundingBoxes from nthreads threads over contiguous sub-ranges of the
+// queries (each range as the SEQ branch does it), concatenated in query order:
+// the same CSR as orc_bvh_find_boxes.
+long long orc_bvh_find_boxes_mt(void* h, const double* q, int m, int* offsets, int* counts, int** cands,
+                                int nthreads)
+{
+  if(nthreads < 1) nthreads = 1;
+  std::vector<int*> part(nthreads, nullptr);
+  std::vector<long long> size(nthreads, 0), lo(nthreads + 1, 0);
+  for(int t = 0; t <= nthreads; ++t) lo[t] = (long long)m * t / nthreads;
+#pragma omp parallel for num_threads(nthreads) schedule(static, 1)
+  for(int t = 0; t < nthreads; ++t)
+    size[t] = orc_bvh_find_boxes(h, q + 6 * lo[t], int(lo[t + 1] - lo[t]), offsets + lo[t], counts + lo[t], &part[t]);
+  long long total = 0;
+  for(int t = 0; t < nthreads; ++t) total += size[t];
+  *cands = static_cast<int*>(std::malloc(sizeof(int) * (total ? total : 1)));
+  long long at = 0;
+  for(int t = 0; t < nthreads; ++t)
+  {
+    for(long long i = lo[t]; i < lo[t + 1]; ++i) offsets[i] += (int)at;
+    if(size[t]) std::memcpy(*cands + at, part[t], sizeof(int) * size[t]);
+    at += size[t];
+    std::free(part[t]);
+  }
+  return total;
+}
+
+// Instrumented findBoundingBoxes: per query, the number of box-predicate calls
+// of the traversal (the roofline numerator counts N_node = calls / 2).
+void orc_bvh_find_boxes_counts(void* h, const double* q, int m, int* box_tests)
+{
+  const Tree& t = *static_cast<Tree*>(h);
+  for(int i = 0; i < m; ++i)
+  {
+    const Box qb = read_box(q + 6 * i);
+    int nb = 0;
+    auto pred = [&](const Box& bb) {
+      ++nb;
+      for(int d = 0; d < 3; ++d)
+        if(!(qb.hi[d] >= bb.lo[d] && qb.lo[d] <= bb.hi[d])) return false;
+      return true;
+    };
+    traverse(t, pred, [](int) {}, [](const Box&, const Box&) { return false; });
+    box_tests[i] = nb;
+  }
+}
+
 long long orc_bvh_find_points(void* h, const double* p, int m, int* offsets, int* counts, int** cands)
 {
   const Tree& t = *static_cast<Tree*>(h);

@@ -126,6 +126,27 @@ long long ref_bvh_find_boxes(void* h, const double* q, int m, int* offsets, int*
   return copy_candidates(c, cands);
 }
 
+// Instrumented findBoundingBoxes: per query, the number of box-predicate
+// calls the BVH's own traverser makes (its generic, no-preference overload,
+// spin/policy/LinearBVH.hpp:91-103, as findBoundingBoxes uses).
+void ref_bvh_find_boxes_counts(void* h, const double* q, int m, int* box_tests)
+{
+  auto* bvh = static_cast<BVHType*>(h);
+  auto it = bvh->getTraverser();
+  std::vector<BoxType> qb = to_boxes(q, m);
+  for(int i = 0; i < m; ++i)
+  {
+    int nb = 0;
+    auto leaf = [](std::int32_t, const std::int32_t*) {};
+    auto pred = [&](const BoxType& query, const BoxType& bb) -> bool {
+      ++nb;
+      return query.intersectsWith(bb);
+    };
+    it.traverse_tree(qb[i], leaf, pred);
+    box_tests[i] = nb;
+  }
+}
+
 long long ref_bvh_find_points(void* h, const double* p, int m, int* offsets, int* counts, int** cands)
 {
   auto* bvh = static_cast<BVHType*>(h);

@@ -7,7 +7,7 @@
 // of the host mirrors.  Linked into an executable with
 // -rdynamic, or preloaded, these definitions take the place of libgsq.so's own,
 // so the host code above them (the quest interface in libgsq.so, the C++ shim
-// include/gsq.hpp, the Python modules) runs on a machine without a GPU, over
+// include/gsq.hpp, the Python classes) runs on a machine without a GPU, over
 // the same results the GPU path gives bit for bit.  Candidates are allocated
 // with malloc, which gsq_free releases for host pointers.  Test infrastructure
 // only.

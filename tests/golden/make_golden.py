@@ -53,6 +53,43 @@ def bvh_fixture(R):
     np.savez_compressed(OUT / "bvh_boxes2000.npz", **out)
 
 
+def bvh_dense_fixture(R):
+    """Queries that hit: over the same 2,000 boxes as bvh_boxes2000, 1,000
+    query boxes 5-400x larger than the inserted ones (sides uniform in
+    [0.05, 0.4]), points inside or on the corners of inserted boxes, and rays
+    aimed at inserted boxes' centres (some along the axes), so the reference's
+    candidate lists, and their order, are dense."""
+    boxes = W.random_boxes(2000, 1)
+    g = W.rng(40)
+    c = g.uniform(0.0, 1.0, size=(1000, 3))
+    side = g.uniform(0.05, 0.4, size=(1000, 3))
+    qboxes = np.concatenate([c - 0.5 * side, c + 0.5 * side], axis=1)
+    pick = g.integers(0, 2000, size=1500)
+    lo, hi = boxes[pick, :3], boxes[pick, 3:]
+    pts = lo + g.uniform(0.0, 1.0, size=(1500, 3)) * (hi - lo)
+    pts[:300] = lo[:300]          # exactly on a corner (inclusive containment)
+    pts[300:500] = hi[300:500]
+    pick = g.integers(0, 2000, size=800)
+    ro = g.uniform(-0.2, 1.2, size=(800, 3))
+    target = 0.5 * (boxes[pick, :3] + boxes[pick, 3:])
+    rd = target - ro
+    ro[:150] = target[:150]       # axis-parallel rays from a box centre
+    rd[:150] = 0.0
+    rd[np.arange(150), np.arange(150) % 3] = np.where(np.arange(150) % 2 == 0, 1.0, -1.0)
+    out = {"boxes": boxes, "query_boxes": qboxes, "points": pts, "ray_origins": ro, "ray_dirs_raw": rd}
+    for scale, tag in ((1.000123, "s"), (1.0, "u")):
+        h = R.bvh(boxes, scale)
+        for k, v in csr(*R.find_boxes(h, qboxes)).items():
+            out[f"{tag}_fb_{k}"] = v
+        for k, v in csr(*R.find_points(h, pts)).items():
+            out[f"{tag}_fp_{k}"] = v
+        off, cnt, cand, dirs = R.find_rays(h, ro, rd)
+        for k, v in csr(off, cnt, cand).items():
+            out[f"{tag}_fr_{k}"] = v
+        out["ray_dirs"] = dirs
+    np.savez_compressed(OUT / "bvh_dense.npz", **out)
+
+
 def sdf_fixture(R, name, v, f, q, watertight=True, sign=True):
     h = R.sdf(v[:, 0], v[:, 1], v[:, 2], f, watertight, sign)
     d, cp, nr = R.sdf_eval(h, q, True, True)
@@ -87,8 +124,12 @@ def main():
     if sys.argv[1:] == ["cp"]:  # only the closest-point fixture
         cp_fixture(R)
         return
+    if sys.argv[1:] == ["bvh_dense"]:  # only the dense candidate fixture
+        bvh_dense_fixture(R)
+        return
     cp_fixture(R)
     bvh_fixture(R)
+    bvh_dense_fixture(R)
     # UV sphere of quest_signed_distance.cpp:86-169 on its 16^3 grid over the
     # sphere box expanded by 2.0
     v, f = W.uv_sphere()

@@ -5,14 +5,23 @@ Workload: level-6 displaced icosphere (81,920 triangles, 40,962 vertices),
 1M points uniform in the 1.2x box, w ~ U[0,1], L = sum_i w_i d_i^2.  Checks:
   * dL/dx against the analytic gradient from the FP64 forward's closest
     points, 2 w (q - cp)  (rtol 1e-10);
-  * dL/dx against FP64 central differences (h = 1e-6) on 1,000 sampled entries;
-  * dL/dV against FP64 central differences on 1,000 sampled entries, using the
-    points whose closest point lies on the vertex's 1-ring (the distance to the
-    ring equals the mesh distance bit for bit there) and the unsigned distance
-    to the perturbed ring (d^2 does not depend on the sign);
+  * dL/dx against central differences (h = 1e-6) of the oracle's FP64
+    distances on 1,000 sampled entries: median relative error <= 1e-9,
+    p99 <= 1e-7, >= 99.8 % within 1e-6 (measured on the oracle alone:
+    median 6e-11, p99 2.6e-9, max 1e-8);
+  * dL/dV against the analytic gradient built on the host from the oracle's
+    closest points, -2 w b_k (q - cp) summed over the points whose closest
+    point lies on the vertex's 1-ring (b_k the barycentric weight of the
+    vertex there): error <= 1e-9 of the sum of |terms|, every sampled entry;
+  * dL/dV against central differences of the oracle's unsigned distance to
+    the perturbed ring over those points, on 1,000 sampled entries: median
+    <= 1e-7, >= 95 % within 1e-6, >= 99 % within 1e-4 of the sum of |terms|
+    (measured on the oracle alone: median 3.7e-9, 97.1 % within 1e-6, p99
+    9.5e-6).  The tail is the points whose closest feature changes within
+    +-h (a closest point within h of a region boundary), where d^2 is C1 but
+    not C2 in the vertex and the central difference errs by about h f'';
   * determinism: two backward calls give identical bits.
-FD tolerance: median relative error <= 1e-5 and >= 97% of entries within 1e-3
-(entries whose closest feature switches within +-h legitimately disagree).
+The measured error percentiles are printed (pytest -s).
 """
 from __future__ import annotations
 
@@ -51,7 +60,7 @@ class SignedDistanceFn:
 
 
 @pytest.fixture(scope="module")
-def case(gsq):
+def case(gsq, port):
     import torch
     v, f = W.displaced_icosphere(6, 1234)
     m = 1 << 20
@@ -60,15 +69,16 @@ def case(gsq):
     sd = gsq.SignedDistance(v, f, precision=axom_gb300.PRECISION_MIXED)
     qd = torch.from_numpy(q).cuda()
     d, cp, _ = sd.compute_distances(qd, closest=True)
-    return dict(v=v, f=f, q=q, w=w, sd=sd, qd=qd, d=d.cpu().numpy(), cp=cp.cpu().numpy())
+    oh = port.sdf(v[:, 0], v[:, 1], v[:, 2], f)
+    return dict(v=v, f=f, q=q, w=w, sd=sd, qd=qd, d=d.cpu().numpy(), cp=cp.cpu().numpy(), oh=oh)
 
 
 def rel_err(a, b):
     return np.abs(a - b) / np.maximum(np.maximum(np.abs(a), np.abs(b)), 1e-12)
 
 
-def fd_ok(err):
-    return np.median(err) <= 1e-5 and np.mean(err <= 1e-3) >= 0.97
+def stats(err):
+    return {"median": float(np.median(err)), "p99": float(np.quantile(err, 0.99)), "max": float(err.max())}
 
 
 def test_grad_points_matches_analytic(gsq, case):
@@ -91,60 +101,77 @@ def test_autograd_function_points(gsq, case):
     assert torch.equal(grad, gp)
 
 
-def test_grad_points_central_differences(gsq, case):
+def test_grad_points_central_differences(gsq, port, case):
     import torch
     rng = W.rng(7)
     idx = rng.choice(case["q"].shape[0], 1000, replace=False)
     comp = rng.integers(0, 3, 1000)
-    sd = case["sd"]
     g = torch.from_numpy(2.0 * case["w"] * case["d"]).cuda()
-    gp, _ = sd.backward(case["qd"], g, want_vertices=False)
+    gp, _ = case["sd"].backward(case["qd"], g, want_vertices=False)
     gp = gp.cpu().numpy()[idx, comp]
     qp = case["q"][idx].copy()
     qm = case["q"][idx].copy()
     qp[np.arange(1000), comp] += H
     qm[np.arange(1000), comp] -= H
-    sd.set_precision(axom_gb300.PRECISION_FP64)
-    dp = sd.compute_distances(qp)
-    dm = sd.compute_distances(qm)
-    sd.set_precision(axom_gb300.PRECISION_MIXED)
+    dp = port.sdf_eval(case["oh"], qp, threads=16)[0]
+    dm = port.sdf_eval(case["oh"], qm, threads=16)[0]
     fd = case["w"][idx] * (dp * dp - dm * dm) / (2 * H)
-    assert fd_ok(rel_err(gp, fd)), (np.median(rel_err(gp, fd)), np.mean(rel_err(gp, fd) <= 1e-3))
+    err = rel_err(gp, fd)
+    st = stats(err)
+    print(f"dL/dx vs oracle central differences: {st}")
+    assert st["median"] <= 1e-9 and st["p99"] <= 1e-7 and np.mean(err <= 1e-6) >= 0.998, st
 
 
-def test_grad_vertices_central_differences(gsq, case):
+def _ring_weight(v, vid, ring, cpts):
+    """Barycentric weight of vertex vid at each closest point, on the ring
+    triangle (every one contains vid) that holds it: the one whose
+    sub-triangle areas sum closest to its own area."""
+    A, B, C = v[ring[:, 0]], v[ring[:, 1]], v[ring[:, 2]]
+    area = np.linalg.norm(np.cross(B - A, C - A), axis=1)
+    P = cpts[:, None, :]
+    wa = np.linalg.norm(np.cross(B - P, C - P), axis=2) / area
+    wb = np.linalg.norm(np.cross(C - P, A - P), axis=2) / area
+    wc = np.linalg.norm(np.cross(A - P, B - P), axis=2) / area
+    k = np.argmin(np.abs(wa + wb + wc - 1.0), axis=1)
+    w3 = np.stack([wa, wb, wc], 2)[np.arange(len(cpts)), k]
+    return (w3 * (ring[k] == vid)).sum(1)
+
+
+def test_grad_vertices_analytic_and_central_differences(gsq, port, case):
     import torch
-    v, f, w = case["v"], case["f"], case["w"]
-    sd = case["sd"]
-    g = torch.from_numpy(2.0 * w * case["d"]).cuda()
-    _, gv = sd.backward(case["qd"], g, want_points=False)
+    v, f, w, q, cp, d = case["v"], case["f"], case["w"], case["q"], case["cp"], case["d"]
+    g = torch.from_numpy(2.0 * w * d).cuda()
+    _, gv = case["sd"].backward(case["qd"], g, want_points=False)
     gv = gv.cpu().numpy()
-    touched = np.flatnonzero(np.abs(gv).sum(1) > 0)
     rng = W.rng(8)
-    verts = rng.choice(touched, 1000, replace=False)
+    verts = rng.choice(np.flatnonzero(np.abs(gv).sum(1) > 0), 1000, replace=False)
     comps = rng.integers(0, 3, 1000)
-    cp, d, q = case["cp"], case["d"], case["q"]
-    errs = []
-    for vid, c in zip(verts, comps):
-        ring = f[np.any(f == vid, axis=1)]
-        rv = v[np.unique(ring)]
-        lo, hi = rv.min(0) - 1e-9, rv.max(0) + 1e-9
-        cand = np.flatnonzero(np.all((cp >= lo) & (cp <= hi), axis=1))
-        if cand.size == 0:
-            continue
-        ring_sd = gsq.SignedDistance(v, ring, is_watertight=False, compute_sign=False)
-        rd = ring_sd.compute_distances(q[cand])
-        on_ring = cand[rd == np.abs(d[cand])]
+    rings = [f[np.any(f == vid, axis=1)] for vid in verts]
+    # points whose closest point lies in a ring's box: the oracle's own BVH over the closest points
+    rbox = np.array([np.concatenate([v[np.unique(r)].min(0) - 1e-9, v[np.unique(r)].max(0) + 1e-9]) for r in rings])
+    off, cnt, cands = port.find_boxes(port.bvh(np.concatenate([cp, cp], 1), 1.0), rbox)
+    g2 = 2.0 * w[:, None] * (q - cp)
+    e_an, e_fd = [], []
+    for i, (vid, c, ring) in enumerate(zip(verts, comps, rings)):
+        cand = np.sort(cands[off[i]:off[i] + cnt[i]])
+        rd = port.sdf_eval(port.sdf(v[:, 0], v[:, 1], v[:, 2], ring, False, False), q[cand])[0]
+        on = cand[rd == np.abs(d[cand])]  # closest point on the ring: the ring's distance is the mesh's
+        assert on.size > 0, vid
+        terms = -_ring_weight(v, vid, ring, cp[on]) * g2[on, c]
+        scale = max(np.abs(terms).sum(), 1e-300)
         vp, vm = v.copy(), v.copy()
         vp[vid, c] += H
         vm[vid, c] -= H
-        rp = gsq.SignedDistance(vp, ring, is_watertight=False, compute_sign=False).compute_distances(q[on_ring])
-        rm = gsq.SignedDistance(vm, ring, is_watertight=False, compute_sign=False).compute_distances(q[on_ring])
-        fd = np.sum(w[on_ring] * (rp * rp - rm * rm)) / (2 * H)
-        errs.append(rel_err(np.array([gv[vid, c]]), np.array([fd]))[0])
-    errs = np.array(errs)
-    assert errs.size >= 900
-    assert fd_ok(errs), (np.median(errs), np.mean(errs <= 1e-3))
+        rp = port.sdf_eval(port.sdf(vp[:, 0], vp[:, 1], vp[:, 2], ring, False, False), q[on])[0]
+        rm = port.sdf_eval(port.sdf(vm[:, 0], vm[:, 1], vm[:, 2], ring, False, False), q[on])[0]
+        fd = np.sum(w[on] * (rp * rp - rm * rm)) / (2 * H)
+        e_an.append(abs(gv[vid, c] - terms.sum()) / scale)
+        e_fd.append(abs(gv[vid, c] - fd) / scale)
+    e_an, e_fd = np.array(e_an), np.array(e_fd)
+    print(f"dL/dV vs host analytic: {stats(e_an)}; vs oracle central differences: {stats(e_fd)}, "
+          f"within 1e-6: {np.mean(e_fd <= 1e-6):.4f}")
+    assert e_an.max() <= 1e-9, stats(e_an)
+    assert np.median(e_fd) <= 1e-7 and np.mean(e_fd <= 1e-6) >= 0.95 and np.mean(e_fd <= 1e-4) >= 0.99, stats(e_fd)
 
 
 def test_backward_is_deterministic(gsq, case):

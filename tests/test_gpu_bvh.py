@@ -51,6 +51,36 @@ def test_find_matches_golden(gsq, scale, tag):
             assert_bits_equal(arr, g[f"{tag}_{key}_{name}"], f"{key} {name}")
 
 
+@pytest.mark.parametrize("scale,tag", [(1.000123, "s"), (1.0, "u")])
+def test_find_matches_dense_golden(gsq, scale, tag):
+    """The reference's candidate lists for queries that hit: 18,721 box
+    candidates (up to 99 per query), points inside and on box corners, rays
+    aimed at boxes and along the axes; offsets, counts and candidate order."""
+    g = golden("bvh_dense")
+    b = gsq.BVH(g["boxes"], scale_factor=scale)
+    for key, res in (("fb", b.find_bounding_boxes(g["query_boxes"])), ("fp", b.find_points(g["points"])),
+                     ("fr", b.find_rays(g["ray_origins"], g["ray_dirs"]))):
+        for name, arr in zip(("offsets", "counts", "candidates"), res):
+            assert_bits_equal(arr, g[f"{tag}_{key}_{name}"], f"{key} {name}")
+
+
+@pytest.mark.parametrize("scale", [1.000123, 1.0])
+def test_config1_full_size_matches_oracle(gsq, port, scale):
+    """The 100,000-box workload at its full size: 100,000 boxes (seed 1),
+    100,000 query boxes (seed 2).  Morton codes, permutation, children, node
+    boxes and bounds, and the whole findBoundingBoxes CSR, bit-exact against
+    the oracle (itself pinned to the reference at this size on the CPU)."""
+    boxes = W.random_boxes(100_000, 1)
+    q = W.random_boxes(100_000, 2)
+    b, h = check_layout(gsq, port, boxes, scale)
+    assert_bits_equal(b.export()[3], port.internals(boxes, scale)["codes"], "codes")
+    got = b.find_bounding_boxes(q)
+    want = port.find_boxes(h, q)
+    for x, y, what in zip(got, want, ("offsets", "counts", "candidates")):
+        assert_bits_equal(x, y, what)
+    assert want[2].size > 4000
+
+
 @pytest.mark.parametrize("n", [0, 1, 2, 3, 5, 17, 100, 4095, 4096, 4097, 50000])
 def test_build_sizes_match_oracle(gsq, port, n):
     boxes = W.random_boxes(n, 100 + n) if n else np.zeros((0, 6))

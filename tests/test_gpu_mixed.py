@@ -86,14 +86,17 @@ def test_mixed_audit_fine_mesh(gsq):
     assert torch.equal(cpm.view(torch.int64), cp64.view(torch.int64))
 
 
-def test_mixed_full_size_near_surface(gsq):
+def test_mixed_full_size_near_surface(gsq, port):
     """Level-8 mesh (1,310,720 triangles), 16M points: half uniform, half at
-    offsets 1e-9..1e-3 along the normal.  Mixed vs FP64 on the GPU: zero sign
-    mismatches and zero relative error; a sample against the oracle."""
+    offsets 1e-9..1e-3 along the normal.  Mixed vs FP64 on the GPU over every
+    point: zero sign mismatches and zero relative error; and a 40,000-point
+    stratified sample (half of it near the surface) against the oracle, bit
+    for bit."""
     import torch
     v, f = W.displaced_icosphere(8, 1234)
     m = 1 << 24
-    q = torch.from_numpy(W.mixed_queries(v, f, m, 4)).cuda()
+    q_host = W.mixed_queries(v, f, m, 4)
+    q = torch.from_numpy(q_host).cuda()
     sd = gsq.SignedDistance(v, f, precision=axom_gb300.PRECISION_FP64)
     d64 = sd.compute_distances(q)
     sd.set_precision(axom_gb300.PRECISION_MIXED)
@@ -102,3 +105,8 @@ def test_mixed_full_size_near_surface(gsq):
     rel = ((dm - d64).abs() / d64.abs().clamp_min(1e-300)).max().item()
     assert rel <= 1e-12
     assert torch.equal(dm.view(torch.int64), d64.view(torch.int64))
+    idx = np.linspace(0, m - 2, 20000).astype(np.int64) // 2 * 2
+    idx = np.concatenate([idx, idx + 1])  # even: uniform, odd: near the surface
+    h = port.sdf(v[:, 0], v[:, 1], v[:, 2], f)
+    pd, _, _ = port.sdf_eval(h, q_host[idx], threads=16)
+    assert_bits_equal(dm[torch.from_numpy(idx).cuda()].cpu().numpy(), pd, "oracle sample")

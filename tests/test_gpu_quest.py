@@ -128,30 +128,3 @@ def test_misuse_after_init_aborts(gsq, tmp_path, call, message):
     assert "before" in p.stdout and "after" not in p.stdout, p.stdout + p.stderr
     assert p.returncode == -signal.SIGABRT, (p.returncode, p.stderr)
     assert message in p.stderr, p.stderr
-
-
-def test_python_module_matches_oracle(gsq, port, tmp_path):
-    """axom_gb300.quest (the reference's Python module functions) over an STL
-    file: the three evaluate forms and the bounds equal the oracle's."""
-    from axom_gb300 import quest
-    v, f = W.displaced_icosphere(2, 9)
-    path = tmp_path / "ico2.stl"
-    write_stl(path, v, f)
-    nodes, cells = gsq.read_stl(path)
-    q = np.concatenate([W.uniform_queries(v, 100, 4), v[:10]])
-    h = port.sdf(nodes[:, 0], nodes[:, 1], nodes[:, 2], cells, True, True)
-    d_ref, cp_ref, n_ref = port.sdf_eval(h, q, True, True)
-    try:
-        assert quest.signed_distance_init(str(path)) == 0, gsq.load().gsq_last_error()
-        d0 = np.array([quest.signed_distance_evaluate(*p) for p in q])
-        assert_bits_equal(d0, d_ref, "evaluate(x, y, z)")
-        r = np.array([quest.signed_distance_evaluate(*p, 0, 0, 0, 0, 0, 0) for p in q])
-        assert_bits_equal(r[:, 0], d_ref, "evaluate with outputs")
-        assert_bits_equal(r[:, 1:4], cp_ref, "closest points")
-        np.testing.assert_allclose(r[:, 4:], n_ref, rtol=0, atol=1e-12)
-        assert_bits_equal(quest.signed_distance_evaluate_points(q[:, 0], q[:, 1], q[:, 2]), d_ref, "array form")
-        lo, hi = quest.signed_distance_get_mesh_bounds()
-        assert_bits_equal(np.concatenate([lo, hi]), np.concatenate([nodes.min(0), nodes.max(0)]), "bounds")
-    finally:
-        quest.signed_distance_finalize()
-    assert not quest.signed_distance_initialized()

@@ -36,6 +36,21 @@ def test_port_find_matches_golden(port, scale, tag):
             assert_bits_equal(arr, g[f"{tag}_{key}_{name}"], f"{key} {name}")
 
 
+@pytest.mark.parametrize("scale,tag", SCALES)
+def test_port_find_matches_dense_golden(port, scale, tag):
+    """Candidate lists the reference made for queries that hit (18,721 box
+    candidates, up to 99 per query; points inside and on the corners of
+    boxes; rays aimed at boxes, some along the axes), order included."""
+    g = golden("bvh_dense")
+    h = port.bvh(g["boxes"], scale)
+    assert_bits_equal(port.normalize_rays(g["ray_dirs_raw"]), g["ray_dirs"], "ray dirs")
+    for key, res in (("fb", port.find_boxes(h, g["query_boxes"])), ("fp", port.find_points(h, g["points"])),
+                     ("fr", port.find_rays(h, g["ray_origins"], g["ray_dirs"]))):
+        for name, arr in zip(("offsets", "counts", "candidates"), res):
+            assert_bits_equal(arr, g[f"{tag}_{key}_{name}"], f"{key} {name}")
+    assert g[f"{tag}_fb_counts"].sum() > 15000
+
+
 def test_port_ray_normalisation_matches_golden(port):
     g = golden("bvh_boxes2000")
     assert_bits_equal(port.normalize_rays(g["ray_dirs_raw"]), g["ray_dirs"], "ray dirs")
@@ -138,6 +153,55 @@ def test_port_matches_reference_small(port, ref, n):
     q = W.random_boxes(300, 7)
     for x, y in zip(port.find_boxes(hp, q), ref.find_boxes(hr, q)):
         assert_bits_equal(x, y, "find boxes")
+
+
+@pytest.mark.parametrize("scale", [1.000123, 1.0])
+def test_port_matches_reference_config1(port, ref, scale):
+    """The 100,000-box workload at its full size: boxes from seed 1, 100,000
+    query boxes from seed 2 (centres U[0,1]^3, sides log-uniform in
+    [1e-3, 1e-2]).  Morton codes, permutation, radix-tree links, parents,
+    inner and leaf boxes, bounds, and the whole findBoundingBoxes CSR
+    (candidate order included) against the reference's SEQ build."""
+    boxes = W.random_boxes(100_000, 1)
+    q = W.random_boxes(100_000, 2)
+    a, b = port.internals(boxes, scale), ref.internals(boxes, scale)
+    for k in a:
+        assert_bits_equal(a[k], b[k], k)
+    hp, hr = port.bvh(boxes, scale), ref.bvh(boxes, scale)
+    assert_bits_equal(port.bounds(hp), ref.bounds(hr), "bounds")
+    got, want = port.find_boxes(hp, q), ref.find_boxes(hr, q)
+    for x, y, what in zip(got, want, ("offsets", "counts", "candidates")):
+        assert_bits_equal(x, y, what)
+    assert want[2].size > 4000
+    # the threaded port (the CPU baseline's all-core form) gives the same CSR
+    for x, y, what in zip(port.find_boxes_mt(hp, q, 7), want, ("offsets", "counts", "candidates")):
+        assert_bits_equal(x, y, f"threaded {what}")
+    # the find roofline's traversal counts, against the reference's own traverser
+    assert_bits_equal(port.find_boxes_counts(hp, q[:20000]), ref.find_boxes_counts(hr, q[:20000]), "box tests")
+
+
+def test_port_matches_reference_level8(port, ref):
+    """The 1,310,720-triangle mesh of the signed-distance benchmark (level-8
+    icosphere, seed 1234): the 20,000-point stratified sample of its 16M
+    uniform points (seed 3) and 20,000 points within 1e-9..1e-3 of the surface.
+    Distances, closest points and normals bit-exact against the reference,
+    and the per-query box and triangle test counts of the uniform sample (the
+    roofline numerator) equal to the reference traverser's."""
+    v, f = W.displaced_icosphere(8, 1234)
+    m = 1 << 24
+    uni = W.uniform_queries(v, m, 3)[np.linspace(0, m - 1, 20000).astype(np.int64)]
+    near = W.near_surface_queries(v, f, 20000, 4)
+    q = np.concatenate([uni, near])
+    hp = port.sdf(v[:, 0], v[:, 1], v[:, 2], f)
+    hr = ref.sdf(v[:, 0], v[:, 1], v[:, 2], f)
+    a = port.sdf_eval(hp, q, True, True, threads=8)
+    b = ref.sdf_eval(hr, q, True, True, threads=8)
+    for x, y, what in zip(a, b, ("distance", "closest", "normals")):
+        assert_bits_equal(x, y, what)
+    nbp, nlp = port.sdf_counts(hp, uni, threads=8)
+    nbr, nlr = ref.sdf_counts(hr, uni, threads=8)
+    assert_bits_equal(nbp, nbr, "box tests")
+    assert_bits_equal(nlp, nlr, "triangle tests")
 
 
 def test_port_matches_reference_edge_cases(port, ref):

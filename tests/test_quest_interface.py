@@ -106,32 +106,6 @@ def test_misuse_aborts_like_the_reference(call, message):
     assert message in p.stderr, p.stderr
 
 
-def test_python_module_mirrors_the_reference_module():
-    """axom_gb300.quest has the functions of the reference's Python module
-    (pyQUESTmodule.cpp:718-760); init fails with -1 on a missing file; an
-    evaluate before init aborts, as there."""
-    from axom_gb300 import quest
-    for name in ("signed_distance_init", "signed_distance_initialized", "signed_distance_set_dimension",
-                 "signed_distance_set_closed_surface", "signed_distance_set_compute_signs",
-                 "signed_distance_set_allocator", "signed_distance_set_verbose",
-                 "signed_distance_use_shared_memory", "signed_distance_set_execution_space",
-                 "signed_distance_evaluate", "signed_distance_finalize"):
-        assert callable(getattr(quest, name)), name
-    p = run_child("""
-        from axom_gb300 import quest
-        assert quest.signed_distance_init("badfile.stl") == -1
-        assert not quest.signed_distance_initialized()
-        quest.signed_distance_set_closed_surface(False)
-        quest.signed_distance_set_execution_space(quest.SignedDistExec_GPU)
-        quest.signed_distance_finalize()
-        print("before", flush=True)
-        quest.signed_distance_evaluate(0.0, 0.0, 0.0)
-        print("after")
-    """)
-    assert "before" in p.stdout and "after" not in p.stdout, p.stdout + p.stderr
-    assert p.returncode == -signal.SIGABRT and "must be initialized" in p.stderr, p.stderr
-
-
 @pytest.fixture(scope="module")
 def mocked_c_caller(tmp_path_factory):
     """tests/cpp/quest_check.c linked with libgsq.so and tests/cpp/oracle_double.cpp,
@@ -170,45 +144,3 @@ def test_misuse_after_init_aborts_on_the_oracle(mocked_c_caller, tmp_path, case,
     assert "before" in p.stdout and "after" not in p.stdout, p.stdout + p.stderr
     assert p.returncode == -signal.SIGABRT, (p.returncode, p.stderr)
     assert message in p.stderr, p.stderr
-
-
-def test_python_module_on_the_oracle(tmp_path):
-    """axom_gb300.quest over libgsq.so with the oracle-backed double preloaded:
-    the three evaluate forms, the result tuple of the second form, the array
-    form and the bounds on the reference's open plane."""
-    inc = ROOT / "include"
-    mock = tmp_path / "liboracle_double.so"
-    subprocess.run(["g++", "-std=c++17", "-O1", "-ffp-contract=off", "-fopenmp", "-fPIC", "-shared", f"-I{inc}",
-                    str(ROOT / "tests/cpp/oracle_double.cpp"), "-o", str(mock)], check=True)
-    stl = tmp_path / "plane.stl"
-    stl.write_text("solid p\n" + "".join(
-        f" facet normal 0 0 1\n  outer loop\n   vertex {a[0]} {a[1]} 0\n   vertex {b[0]} {b[1]} 0\n"
-        "   vertex 0 0 0\n  endloop\n endfacet\n"
-        for a, b in (((5, -5), (5, 5)), ((5, 5), (-5, 5)), ((-5, 5), (-5, -5)), ((-5, -5), (5, -5)))) + "endsolid p\n")
-    code = textwrap.dedent(f"""
-        import numpy as np
-        from axom_gb300 import quest
-        quest.signed_distance_set_closed_surface(False)
-        assert quest.signed_distance_init({str(stl)!r}) == 0
-        assert quest.signed_distance_initialized()
-        g = np.linspace(-4.0, 4.0, 16)
-        x, y, z = (a.ravel() for a in np.meshgrid(g, g, g, indexing="ij"))
-        phi = quest.signed_distance_evaluate_points(x, y, z)
-        np.testing.assert_array_max_ulp(phi, z, maxulp=4)
-        for i in range(0, x.size, 97):
-            assert quest.signed_distance_evaluate(x[i], y[i], z[i]) == phi[i]
-            r = quest.signed_distance_evaluate(x[i], y[i], z[i], 0, 0, 0, 0, 0, 0)
-            assert len(r) == 7 and r[0] == phi[i]
-            assert np.allclose(r[1:4], (x[i], y[i], 0.0), rtol=0, atol=1e-12)
-            assert np.allclose(r[4:], (0.0, 0.0, 1.0), rtol=0, atol=1e-12)
-        lo, hi = quest.signed_distance_get_mesh_bounds()
-        assert list(lo) == [-5.0, -5.0, 0.0] and list(hi) == [5.0, 5.0, 0.0]
-        quest.signed_distance_finalize()
-        assert not quest.signed_distance_initialized()
-        print("OK")
-    """)
-    from axom_gb300 import build
-    build.build()
-    env = dict(os.environ, LD_PRELOAD=str(mock))
-    p = subprocess.run([sys.executable, "-c", code], capture_output=True, text=True, timeout=300, cwd=ROOT, env=env)
-    assert p.returncode == 0 and "OK" in p.stdout, p.stdout + p.stderr

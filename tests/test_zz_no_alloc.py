@@ -1,9 +1,9 @@
 """GPU: the allocation-free entry point gsq_sdf_eval_noalloc.
 
 It exists for callers that must not allocate device memory while they
-evaluate (a pool allocator that owns all device memory, evaluation inside a
-CUDA stream capture, latency-bound loops that cannot take cudaMalloc's
-device-wide synchronisation).  Its only scratch is a fixed array in the
+evaluate (an application whose pool allocator owns all device memory, or
+other streams that must not be stalled by cudaMalloc's device-wide
+synchronisation).  Its only scratch is a fixed array in the
 library's device image shared by all calls, so this test calls it twice in a
 row on different point sets and checks each call against gsq_sdf_eval, with
 the tolerance the other signed-distance tests use (bit-exact distances).  It
