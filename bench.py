@@ -63,6 +63,8 @@ def parse():
     ap.add_argument("--precision", default="mixed", choices=["mixed", "fp64"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--cpu-seconds", type=float, default=10.0)
+    ap.add_argument("--only-config1", action="store_true",
+                    help="run only the 100,000-box build and find leg (for profiling); prints its object")
     ap.add_argument("--no-forms", dest="forms", action="store_false",
                     help="skip the near-surface and adjoint legs")
     ap.add_argument("--batch-meshes", type=int, default=BATCH_MESHES,
@@ -492,6 +494,9 @@ def run_gsq(args, world, rank, local):
 
     torch.cuda.set_device(local)
     torch.cuda.init()
+    if args.only_config1:
+        print(json.dumps(config1_leg(args, G, torch, oracle.Port(), os.cpu_count() or 1)), flush=True)
+        return
     dist = None
     if world > 1:
         import torch.distributed as dist
