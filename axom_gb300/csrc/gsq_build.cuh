@@ -19,13 +19,18 @@ struct ArgV
   double v;
   int i;
 };
+// (comparisons on the integer pipe, OKey, with the FP64 outcomes)
 __device__ __forceinline__ void take_min(ArgV& a, const ArgV& b)
 {
-  if(b.i != INT_MAX && (a.i == INT_MAX || b.v < a.v || (b.v == a.v && b.i < a.i))) a = b;
+  if(b.i == INT_MAX) return;
+  const OKey kb = okey(b.v), ka = okey(a.v);
+  if(a.i == INT_MAX || ok_lt(kb, ka) || (ok_eq(kb, ka) && b.i < a.i)) a = b;
 }
 __device__ __forceinline__ void take_max(ArgV& a, const ArgV& b)
 {
-  if(b.i != INT_MAX && (a.i == INT_MAX || b.v > a.v || (b.v == a.v && b.i < a.i))) a = b;
+  if(b.i == INT_MAX) return;
+  const OKey kb = okey(b.v), ka = okey(a.v);
+  if(a.i == INT_MAX || ok_gt(kb, ka) || (ok_eq(kb, ka) && b.i < a.i)) a = b;
 }
 __device__ __forceinline__ ArgV shfl_argv(const ArgV& a, int src)
 {
@@ -95,7 +100,9 @@ __device__ __forceinline__ Fold fold_block(Fold f)
 // Invalid boxes are left as they are.  Returns the box's validity.
 __device__ __forceinline__ bool scale_box(double* lo, double* hi, double half)
 {
-  const bool valid = box_valid(lo, hi);
+  const OKey kl[3] = {okey(lo[0]), okey(lo[1]), okey(lo[2])};
+  const OKey kh[3] = {okey(hi[0]), okey(hi[1]), okey(hi[2])};
+  const bool valid = box_valid_k(kl, kh);
   if(valid)
   {
     for(int d = 0; d < 3; ++d)
@@ -106,7 +113,7 @@ __device__ __forceinline__ bool scale_box(double* lo, double* hi, double half)
       hi[d] = mid + r;
     }
     for(int d = 0; d < 3; ++d)
-      if(lo[d] > hi[d])
+      if(ok_gt(okey(lo[d]), okey(hi[d])))
       {
         const double t = lo[d];
         lo[d] = hi[d];
@@ -124,7 +131,7 @@ __device__ __forceinline__ void fold_add_box(Fold& f, const double* lo, const do
   for(int d = 0; d < 3; ++d)
   {
     take_min(f.lo[d], ArgV {lo[d], i});
-    take_max(f.hi[d], ArgV {(lo[d] == hi[d]) ? lo[d] : hi[d], i});
+    take_max(f.hi[d], ArgV {ok_eq(okey(lo[d]), okey(hi[d])) ? lo[d] : hi[d], i});
   }
   f.first_valid = min(f.first_valid, i);
 }
@@ -254,22 +261,39 @@ __device__ __forceinline__ void karras_node(int i, const uint32_t* __restrict__ 
   if(i == 0) parent[0] = -1;
 }
 
-// BoundingBox::addBox (BoundingBox.hpp:487-505) into acc.
+// BoundingBox::addBox (BoundingBox.hpp:487-505) into acc (comparisons on the
+// integer pipe, OKey, with the FP64 outcomes).
 __device__ __forceinline__ void add_box(double* alo, double* ahi, const double* lo, const double* hi)
 {
-  if(box_valid(alo, ahi))
+  OKey ka[3], kb[3], kl[3], kh[3];
+  for(int d = 0; d < 3; ++d)
   {
-    if(box_valid(lo, hi))
+    ka[d] = okey(alo[d]);
+    kb[d] = okey(ahi[d]);
+    kl[d] = okey(lo[d]);
+    kh[d] = okey(hi[d]);
+  }
+  if(box_valid_k(ka, kb))
+  {
+    if(box_valid_k(kl, kh))
     {
       for(int d = 0; d < 3; ++d)
       {
-        if(lo[d] < alo[d]) alo[d] = lo[d];
-        if(lo[d] > ahi[d]) ahi[d] = lo[d];
+        if(ok_lt(kl[d], ka[d]))
+        {
+          alo[d] = lo[d];
+          ka[d] = kl[d];
+        }
+        if(ok_gt(kl[d], kb[d]))
+        {
+          ahi[d] = lo[d];
+          kb[d] = kl[d];
+        }
       }
       for(int d = 0; d < 3; ++d)
       {
-        if(hi[d] < alo[d]) alo[d] = hi[d];
-        if(hi[d] > ahi[d]) ahi[d] = hi[d];
+        if(ok_lt(kh[d], ka[d])) alo[d] = hi[d];
+        if(ok_gt(kh[d], kb[d])) ahi[d] = hi[d];
       }
     }
   }
@@ -281,10 +305,21 @@ __device__ __forceinline__ void add_box(double* alo, double* ahi, const double* 
     }
 }
 
+// atomicAdd with acquire-release ordering at device scope: the caller's
+// earlier stores are visible to whoever reads the counter's new value, and
+// the caller sees the stores of the threads whose increments it read.
+__device__ __forceinline__ int atomic_add_acq_rel(int* p, int v)
+{
+  int old;
+  asm volatile("atom.acq_rel.gpu.global.add.s32 %0, [%1], %2;" : "=r"(old) : "l"(p), "r"(v) : "memory");
+  return old;
+}
+
 // propagate_aabbs (BR:505-576) fused with emit_bvh_parents (LB:225-264), for
 // sorted leaf k with box (lo, hi) of a hierarchy over n leaves.  The thread
-// stores its box into its parent's record, fences, and bumps the parent's
-// counter; the first arrival exits and the second combines the two child
+// stores its box into its parent's record and bumps the parent's counter with
+// an acquire-release atomic (the store is visible to the second arrival, which
+// sees the first arrival's box); the first arrival exits and the second combines the two child
 // boxes as the reference's SEQ order does (box(node) = addBox(box(right),
 // box(left))) and moves up.  No thread ever waits on another.
 __device__ __forceinline__ void refit_leaf(int k, double* lo, double* hi, int n, const int* __restrict__ lchild,
@@ -303,9 +338,7 @@ __device__ __forceinline__ void refit_leaf(int k, double* lo, double* hi, int n,
       dst[d] = lo[d];
       dst[3 + d] = hi[d];
     }
-    __threadfence();
-    if(atomicAdd(&counters[node], 1) == 0) return;
-    __threadfence();
+    if(atomic_add_acq_rel(&counters[node], 1) == 0) return;
     const double* b = nodes[node].b;
     double llo[3], lhi[3];
     for(int d = 0; d < 3; ++d)

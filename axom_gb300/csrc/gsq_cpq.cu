@@ -11,8 +11,10 @@
 // found wins ties).  Not found: index and domain -1, position and distance NaN.
 //
 // Two forms, equal bit for bit: FP64 (every decision in FP64, the reference's
-// operation order), and mixed (node decisions certified in FP32 on outward
-// rounded boxes, undecided ones and every point distance in FP64).
+// operation order), and mixed: a persistent warp loop (k_cpq_persist) whose
+// node decisions are certified in FP32 on outward rounded boxes and whose
+// leaf actions are certified on FP32 enclosures of the points' FP64 squared
+// distances; what FP32 cannot decide runs in FP64, converged across the warp.
 #include "gsq_sdf_handle.cuh"
 
 #include <algorithm>
@@ -38,6 +40,15 @@ struct __align__(16) PointRec
 };
 static_assert(sizeof(PointRec) == 32, "point record is 32 bytes");
 
+// The same leaf for the FP32 certificate: the point rounded to nearest and
+// its index (-1 for the padding leaf of a 0/1-point cloud).
+struct __align__(16) PointRec32
+{
+  float p[3];
+  int id;
+};
+static_assert(sizeof(PointRec32) == 16, "fp32 point record is 16 bytes");
+
 __global__ void k_point_boxes(const double* __restrict__ pts, int n, double* __restrict__ boxes)
 {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -62,6 +73,17 @@ __global__ void k_point_records(const int* __restrict__ perm, int nleaves, const
   r.id = ok ? c : -1;
   r.dom = (ok && dom) ? dom[c] : (ok ? 0 : -1);
   recs[k] = r;
+}
+
+__global__ void k_point_records32(const PointRec* __restrict__ recs, int nleaves, PointRec32* __restrict__ out)
+{
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if(k >= nleaves) return;
+  const PointRec r = recs[k];
+  PointRec32 o;
+  for(int d = 0; d < 3; ++d) o.p[d] = __double2float_rn(r.p[d]);
+  o.id = r.id;
+  out[k] = o;
 }
 
 __global__ void k_cpq_codes(const double* __restrict__ q, int m, const double* b, uint32_t* __restrict__ codes)
@@ -119,15 +141,13 @@ __device__ __forceinline__ void cpq_visit_fp64(const NodeRec64* __restrict__ nod
   }
 }
 
-template <bool MIXED>
+// The FP64 form: one thread per query, every decision in FP64.
 __global__ void __launch_bounds__(128) k_cpq(const NodeRec64* __restrict__ nodes64,
-                                             const NodeRec32* __restrict__ nodes32,
                                              const PointRec* __restrict__ recs,
                                              const double* __restrict__ qs,
                                              int m,
                                              const int* __restrict__ order,
                                              double thr,
-                                             float coord_max,
                                              int* __restrict__ out_idx,
                                              int* __restrict__ out_dom,
                                              double* __restrict__ out_pos,
@@ -139,15 +159,8 @@ __global__ void __launch_bounds__(128) k_cpq(const NodeRec64* __restrict__ nodes
   const int i = order ? __ldg(order + t) : t;
   const double q[3] = {qs[3 * (size_t)i], qs[3 * (size_t)i + 1], qs[3 * (size_t)i + 2]};
   double best = DBL_MAX;
-  int bid = -1, bdom = -1, bleaf = -1;
-  QCtx c;
-  if(MIXED)
-  {
-    qctx_init(c, q, coord_max);
-    qctx_update(c, fmin(best, thr));
-  }
+  int bleaf = -1;
   auto visit = [&](int cur, bool& inL, bool& inR, bool& swap, int2& ch) {
-    if(MIXED && visit32(nodes32, cur, c, inL, inR, swap, ch)) return;
     ch = __ldg(reinterpret_cast<const int2*>(nodes64[cur].child));
     cpq_visit_fp64(nodes64, cur, q, best, thr, inL, inR, swap);
   };
@@ -158,22 +171,283 @@ __global__ void __launch_bounds__(128) k_cpq(const NodeRec64* __restrict__ nodes
     if(sq < best)
     {
       best = sq;
-      bid = r.id;
-      bdom = r.dom;
       bleaf = leafpos;
-      if(MIXED) qctx_update(c, fmin(best, thr));
     }
   };
   if(!traverse_point(visit, leaf)) atomicOr(err, DEVERR_STACK);
-  out_idx[i] = bid;
-  out_dom[i] = bdom;
   const double nan = __longlong_as_double(0x7ff8000000000000LL);
   const PointRec* r = (bleaf >= 0) ? recs + bleaf : nullptr;
+  out_idx[i] = r ? r->id : -1;
+  out_dom[i] = r ? r->dom : -1;
   for(int d = 0; d < 3; ++d) out_pos[3 * (size_t)i + d] = r ? r->p[d] : nan;
   out_dist[i] = r ? sqrt(best) : nan;
 }
 
+// The mixed form as a persistent warp loop over Morton-ordered queries.  Each
+// lane runs one query's traversal (the reference's point traverser, deferred
+// leaves included) as a resumable state machine; an iteration takes the
+// deferred leaf where the descent stopped, then one node visit, both decided
+// in FP32 where FP32 can prove the FP64 outcome:
+//  * node: visit32 against an FP32 interval holding min(best, threshold);
+//  * leaf: the point's FP64 squared distance lies in [lo2, hi2]
+//    (point_bounds32).  lo2 >= the interval's top: "sq < best" is certainly
+//    false, nothing happens.  Otherwise the leaf is queued (up to QC per
+//    lane) and the interval narrows to the minimum over the resolved best
+//    and the queue; a leaf with hi2 below the interval's bottom is certainly
+//    closer than everything before it and supersedes the queue and the
+//    resolved best (replaying them would end in this leaf anyway).
+// A lane parks when a node decision is uncertain, its queue is full, or its
+// traversal ends; once enough lanes are parked (the batch size rule of the
+// signed-distance kernel) the warp replays the parked lanes' queues in FP64
+// in order ("replace the best if strictly closer"), runs their uncertain node
+// visits in FP64 and writes finished queries, converged.
+constexpr float CPQ_BATCH_K = 38.5f, CPQ_LAM0 = 0.1f;
+constexpr int CPQ_BATCH_LO = 8, CPQ_BATCH_HI = 24;
+
+template <int QC>
+__global__ void __launch_bounds__(128) k_cpq_persist(const NodeRec64* __restrict__ nodes64,
+                                                     const NodeRec32* __restrict__ nodes32,
+                                                     const PointRec* __restrict__ recs,
+                                                     const PointRec32* __restrict__ recs32,
+                                                     const double* __restrict__ qs,
+                                                     int m,
+                                                     const int* __restrict__ order,
+                                                     double thr,
+                                                     float coord_max,
+                                                     int* __restrict__ out_idx,
+                                                     int* __restrict__ out_dom,
+                                                     double* __restrict__ out_pos,
+                                                     double* __restrict__ out_dist,
+                                                     int* err,
+                                                     int* __restrict__ work)
+{
+  constexpr unsigned FULL = 0xFFFFFFFFu;
+  constexpr int M_DESCEND = 0, M_LEAF = 1, M_IDLE = 2;
+  constexpr int P_NONE = 0, P_NODE = 1, P_FLUSH = 2, P_FINISH = 3;
+  const int lane = threadIdx.x & 31;
+  const unsigned lt_mask = (1u << lane) - 1u;
+  const float thr_lo = fp::f_rd(thr), thr_hi = fp::f_ru(thr);
+  int idx = 0;
+  double q[3] = {0.0, 0.0, 0.0};
+  QCtx c;
+  double best = DBL_MAX;  // the resolved state: best squared distance and its leaf
+  int bleaf = -1;
+  float blo = FLT_MAX, bhi = INFINITY;  // best rounded down and up
+  int pq[QC];                           // queued leaves, in traversal order
+  int np = 0;
+  float plo = INFINITY, phi = INFINITY;  // bounds on the queued leaves' smallest squared distance
+  bool reset = false;                    // a queued leaf superseded the resolved state
+  int todo[STACK_SIZE];
+  todo[0] = BARRIER;
+  int sp = 0, found = 0, cur = 0;
+  int mode = M_IDLE, pend = P_NONE;
+  int2 pch = make_int2(0, 0);
+  bool open = true;
+  float lam = CPQ_LAM0;
+  int bmin = 12, since = 0;
+
+  auto set_thresholds = [&]() {
+    const float lo = fminf(reset ? INFINITY : blo, plo), hi = fminf(reset ? INFINITY : bhi, phi);
+    qctx_set32(c, fminf(lo, thr_lo), fminf(hi, thr_hi));
+  };
+  auto resolved = [&]() {
+    blo = fp::f_rd(best);
+    bhi = fp::f_ru(best);
+    reset = false;
+    np = 0;
+    plo = phi = INFINITY;
+    set_thresholds();
+  };
+  auto pop = [&]() { return (sp >= 0) ? todo[sp--] : BARRIER; };
+  auto apply_visit = [&](bool inL, bool inR, bool swap, int2 ch) {
+    if(!inL && !inR)
+      cur = pop();
+    else
+    {
+      cur = inL ? ch.x : ch.y;
+      int rc = ch.y;
+      if(inL && inR)
+      {
+        if(swap)
+        {
+          const int tmp = cur;
+          cur = rc;
+          rc = tmp;
+        }
+        if(sp + 1 >= STACK_SIZE)
+        {
+          atomicOr(err, DEVERR_STACK);
+          pend = P_FINISH;
+          return;
+        }
+        todo[++sp] = rc;
+      }
+    }
+    if(cur < 0 && !(found < 0))
+    {
+      found = cur;
+      if(cur != BARRIER) cur = pop();
+    }
+  };
+  auto after_leaf = [&]() {
+    found = cur;
+    if(cur < 0 && cur != BARRIER) cur = pop();
+  };
+
+  while(true)
+  {
+    const unsigned want = __ballot_sync(FULL, mode == M_IDLE && open);
+    if(want)
+    {
+      const int leader = __ffs(want) - 1;
+      int base = 0;
+      if(lane == leader) base = atomicAdd(work, __popc(want));
+      base = __shfl_sync(FULL, base, leader);
+      if(mode == M_IDLE && open)
+      {
+        const int t = base + __popc(want & lt_mask);
+        if(t < m)
+        {
+          idx = order ? __ldg(order + t) : t;
+          for(int d = 0; d < 3; ++d) q[d] = qs[3 * (size_t)idx + d];
+          qctx_init(c, q, coord_max);
+          best = DBL_MAX;
+          bleaf = -1;
+          resolved();
+          sp = 0;
+          todo[0] = BARRIER;
+          found = 0;
+          cur = 0;
+          mode = M_DESCEND;
+          pend = P_NONE;
+        }
+        else
+          open = false;
+      }
+    }
+    const unsigned live = __ballot_sync(FULL, mode != M_IDLE);
+    if(live == 0) break;
+    const unsigned parked = __ballot_sync(FULL, pend != P_NONE);
+    ++since;
+    if(parked && (parked == live || __popc(parked) >= bmin))
+    {
+      lam = 0.875f * lam + 0.125f * (float)__popc(parked) / (float)since;
+      bmin = (int)fminf(fmaxf(CPQ_BATCH_K * sqrtf(lam), (float)CPQ_BATCH_LO), (float)CPQ_BATCH_HI);
+      since = 0;
+      const int p = pend;
+      pend = P_NONE;
+      if(p != P_NONE)
+      {
+        // the queued leaf actions in FP64, in order (DistributedClosestPointImpl.hpp:1031-1040)
+        if(reset)
+        {
+          best = DBL_MAX;
+          bleaf = -1;
+        }
+        for(int j = 0; j < np; ++j)
+        {
+          const PointRec r = recs[pq[j]];
+          if(r.id < 0) continue;
+          const double sq = sqdist_pp(q, r.p);
+          if(sq < best)
+          {
+            best = sq;
+            bleaf = pq[j];
+          }
+        }
+        resolved();
+      }
+      if(p == P_NODE)
+      {
+        bool inL, inR, swap;
+        cpq_visit_fp64(nodes64, cur, q, best, thr, inL, inR, swap);
+        apply_visit(inL, inR, swap, pch);
+      }
+      else if(p == P_FINISH)
+      {
+        const double nan = __longlong_as_double(0x7ff8000000000000LL);
+        const PointRec* r = (bleaf >= 0) ? recs + bleaf : nullptr;
+        out_idx[idx] = r ? r->id : -1;
+        out_dom[idx] = r ? r->dom : -1;
+        for(int d = 0; d < 3; ++d) out_pos[3 * (size_t)idx + d] = r ? r->p[d] : nan;
+        out_dist[idx] = r ? sqrt(best) : nan;
+        mode = M_IDLE;
+      }
+      continue;
+    }
+    if(mode == M_IDLE || pend != P_NONE) continue;
+    if(mode == M_DESCEND && cur < 0) mode = M_LEAF;
+    if(mode == M_LEAF)
+    {
+      if(found < 0 && found != BARRIER)
+      {
+        const int lp = -found - 1;
+        const float4 rv = __ldg(reinterpret_cast<const float4*>(recs32 + lp));
+        if(__float_as_int(rv.w) >= 0)
+        {
+          const float pf[3] = {rv.x, rv.y, rv.z};
+          float lo2, hi2;
+          point_bounds32(c, pf, lo2, hi2);
+          const float cur_lo = fminf(reset ? INFINITY : blo, plo), cur_hi = fminf(reset ? INFINITY : bhi, phi);
+          if(!(lo2 >= cur_hi))
+          {
+            if(hi2 < cur_lo)
+            {
+              np = 0;
+              plo = phi = INFINITY;
+              reset = true;
+            }
+            pq[np++] = lp;
+            if(np == QC)
+              pend = P_FLUSH;
+            else
+            {
+              plo = fminf(plo, lo2);
+              phi = fminf(phi, hi2);
+              set_thresholds();
+            }
+          }
+        }
+        after_leaf();
+      }
+      if(pend == P_NONE && !(found < 0 && found != BARRIER))
+      {
+        found = 0;
+        if(cur == BARRIER)
+          pend = P_FINISH;
+        else
+          mode = M_DESCEND;
+      }
+    }
+    if(mode == M_DESCEND && pend == P_NONE && cur >= 0)
+    {
+      bool inL, inR, swap;
+      int2 ch;
+      if(visit32(nodes32, cur, c, inL, inR, swap, ch))
+        apply_visit(inL, inR, swap, ch);
+      else
+      {
+        pend = P_NODE;
+        pch = ch;
+      }
+    }
+  }
+}
+
 inline int grid_for(long long n, int threads) { return (int)std::max<long long>(1, (n + threads - 1) / threads); }
+
+// Grid of the persistent kernel: as many blocks as fit on the device, at most
+// one per `threads` queries.
+template <class K>
+cudaError_t persist_grid(K kernel, int threads, long long m, int* grid)
+{
+  int dev = 0, sms = 0, per_sm = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if(e == cudaSuccess) e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  if(e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, threads, 0);
+  *grid = (int)std::max<long long>(1, std::min<long long>((long long)sms * std::max(per_sm, 1), (m + threads - 1) / threads));
+  return e;
+}
 }  // namespace
 }  // namespace gsq
 
@@ -185,7 +459,9 @@ struct gsq_cpq
   int n = 0;
   gsq_bvh* bvh = nullptr;
   PointRec* recs = nullptr;
+  PointRec32* recs32 = nullptr;
   NodeRec32* nodes32 = nullptr;
+  int* d_work = nullptr;  // work-queue counter of the persistent query kernel
   double* d_bounds = nullptr;
   float coord_max = 0.f;
   int* d_err = nullptr;
@@ -197,6 +473,8 @@ namespace
 void cpq_release(gsq_cpq* h)
 {
   if(h->recs) cudaFree(h->recs);
+  if(h->recs32) cudaFree(h->recs32);
+  if(h->d_work) cudaFree(h->d_work);
   if(h->nodes32) cudaFree(h->nodes32);
   if(h->d_bounds) cudaFree(h->d_bounds);
   if(h->d_err) cudaFree(h->d_err);
@@ -244,11 +522,14 @@ int gsq_cpq_create(gsq_cpq** out, const double* points, int32_t n, const int32_t
   if(rc) return bail(rc);
   const BvhDev* B = bvh_dev(h->bvh);
   e = cudaMalloc(&h->recs, sizeof(PointRec) * B->n);
+  if(e == cudaSuccess) e = cudaMalloc(&h->recs32, sizeof(PointRec32) * B->n);
+  if(e == cudaSuccess) e = cudaMalloc(&h->d_work, sizeof(int));
   if(e == cudaSuccess) e = cudaMalloc(&h->nodes32, sizeof(NodeRec32) * std::max(B->n - 1, 1));
   if(e != cudaSuccess) return bail(cuda_fail(e, "gsq_cpq_create: records"));
   k_point_records<<<grid_for(B->n, 256), 256, 0, s>>>(B->perm, B->n, static_cast<const double*>(pb.dev),
                                                       static_cast<const int*>(db.dev), n, h->recs);
-  count_launch();
+  k_point_records32<<<grid_for(B->n, 256), 256, 0, s>>>(h->recs, B->n, h->recs32);
+  count_launch(2);
   rc = mixed_prepare(B->nodes, B->n - 1, nullptr, 0, 3, h->nodes32, nullptr, s);
   if(rc) return bail(rc);
   double mm = 0.0;
@@ -312,14 +593,19 @@ int gsq_cpq_query(const gsq_cpq* hc, const double* points, int32_t m, double sq_
   GSQ_CUDA_TRY(cudaEventCreate(&e1));
   cudaEventRecord(e0, s);
   if(precision == GSQ_PRECISION_MIXED)
-    k_cpq<true><<<grid_for(m, 128), 128, 0, s>>>(B->nodes, h->nodes32, h->recs, q, m, order, sq_threshold,
-                                                 h->coord_max, static_cast<int*>(ib.dev), static_cast<int*>(dmb.dev),
-                                                 static_cast<double*>(pb.dev), static_cast<double*>(sb.dev), h->d_err);
+  {
+    auto kernel = k_cpq_persist<2>;
+    int g = 1;
+    GSQ_CUDA_TRY(persist_grid(kernel, 128, m, &g));
+    GSQ_CUDA_TRY(cudaMemsetAsync(h->d_work, 0, sizeof(int), s));
+    kernel<<<g, 128, 0, s>>>(B->nodes, h->nodes32, h->recs, h->recs32, q, m, order, sq_threshold, h->coord_max,
+                             static_cast<int*>(ib.dev), static_cast<int*>(dmb.dev), static_cast<double*>(pb.dev),
+                             static_cast<double*>(sb.dev), h->d_err, h->d_work);
+  }
   else
-    k_cpq<false><<<grid_for(m, 128), 128, 0, s>>>(B->nodes, h->nodes32, h->recs, q, m, order, sq_threshold,
-                                                  h->coord_max, static_cast<int*>(ib.dev),
-                                                  static_cast<int*>(dmb.dev), static_cast<double*>(pb.dev),
-                                                  static_cast<double*>(sb.dev), h->d_err);
+    k_cpq<<<grid_for(m, 128), 128, 0, s>>>(B->nodes, h->recs, q, m, order, sq_threshold, static_cast<int*>(ib.dev),
+                                           static_cast<int*>(dmb.dev), static_cast<double*>(pb.dev),
+                                           static_cast<double*>(sb.dev), h->d_err);
   count_launch();
   cudaEventRecord(e1, s);
   cudaError_t e = cudaGetLastError();

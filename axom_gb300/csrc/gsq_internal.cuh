@@ -176,6 +176,22 @@ struct BvhDev
   double bounds[6];               // host copy of the global bounds
   void* block = nullptr;          // single allocation backing the arrays
   size_t block_bytes = 0;
+  // Build scratch and staging, kept between builds (grow-only), and the
+  // build captured as a CUDA graph: a build with the same inputs as the one
+  // before it (count, scale, box array, error word) replays the graph.
+  void* work = nullptr;
+  size_t work_bytes = 0;
+  void* stage = nullptr;          // host boxes copied to the device
+  size_t stage_bytes = 0;
+  double* pad = nullptr;          // the two boxes of a 0/1-box build
+  cudaStream_t cs = nullptr;      // private stream the build is captured on
+  cudaGraphExec_t exec = nullptr;
+  int graph_kernels = 0;
+  int key_n = -1;                 // inputs of the last build
+  double key_scale = 0.0;
+  const double* key_in = nullptr;
+  int* key_err = nullptr;
+  void drop_graph();
   void release();
 };
 
@@ -214,6 +230,52 @@ __host__ __device__ inline bool box_valid(const double* lo, const double* hi)
 {
   // BoundingBox::isValid (primal/geometry/BoundingBox.hpp:451-460)
   return !(lo[0] > hi[0] || lo[1] > hi[1] || lo[2] > hi[2]);
+}
+
+// ---- exact FP64 comparisons on the integer pipe ----------------------------
+// This GPU executes FP64 instructions, comparisons included, at a small
+// fraction of its FP32/integer rate, so comparison-heavy loops (box tests,
+// addBox, the bounds fold) compare doubles through their bit patterns: for
+// non-NaN x, y the map  k(x) = b ^ ((b >> 63) & INT64_MAX)  (b the bits, with
+// -0 taken as +0) is strictly increasing, so x < y exactly when k(x) < k(y)
+// and x == y exactly when k(x) == k(y).  Any comparison involving a NaN is
+// false, as in IEEE arithmetic; the results equal the FP64 comparisons.
+struct OKey
+{
+  long long k;
+  bool nan;
+};
+
+__host__ __device__ inline long long dbits(double x)
+{
+#ifdef __CUDA_ARCH__
+  return __double_as_longlong(x);
+#else
+  long long b;
+  __builtin_memcpy(&b, &x, sizeof b);
+  return b;
+#endif
+}
+
+__host__ __device__ inline OKey okey(double x)
+{
+  long long b = dbits(x);
+  OKey r;
+  r.nan = (b & 0x7FFFFFFFFFFFFFFFLL) > 0x7FF0000000000000LL;
+  if(b == (long long)0x8000000000000000ULL) b = 0;
+  r.k = b ^ ((b >> 63) & 0x7FFFFFFFFFFFFFFFLL);
+  return r;
+}
+__host__ __device__ inline bool ok_lt(const OKey& a, const OKey& b) { return !(a.nan | b.nan) && a.k < b.k; }
+__host__ __device__ inline bool ok_gt(const OKey& a, const OKey& b) { return !(a.nan | b.nan) && a.k > b.k; }
+__host__ __device__ inline bool ok_le(const OKey& a, const OKey& b) { return !(a.nan | b.nan) && a.k <= b.k; }
+__host__ __device__ inline bool ok_ge(const OKey& a, const OKey& b) { return !(a.nan | b.nan) && a.k >= b.k; }
+__host__ __device__ inline bool ok_eq(const OKey& a, const OKey& b) { return !(a.nan | b.nan) && a.k == b.k; }
+
+// box_valid on keys
+__host__ __device__ inline bool box_valid_k(const OKey* lo, const OKey* hi)
+{
+  return !(ok_gt(lo[0], hi[0]) || ok_gt(lo[1], hi[1]) || ok_gt(lo[2], hi[2]));
 }
 
 __host__ __device__ inline double dot3(double u0, double u1, double u2, double v0, double v1, double v2)

@@ -35,6 +35,7 @@ GSQ_HD float mul_ru(float a, float b) { return __fmul_ru(a, b); }
 GSQ_HD float mul_rd(float a, float b) { return __fmul_rd(a, b); }
 GSQ_HD float div_ru(float a, float b) { return __fdiv_ru(a, b); }
 GSQ_HD float sqrt_ru(float a) { return __fsqrt_ru(a); }
+GSQ_HD float sqrt_rd(float a) { return __fsqrt_rd(a); }
 GSQ_HD float f_rn(double a) { return __double2float_rn(a); }
 GSQ_HD float f_ru(double a) { return __double2float_ru(a); }
 GSQ_HD float f_rd(double a) { return __double2float_rd(a); }
@@ -50,6 +51,11 @@ GSQ_HD float sqrt_ru(float a)
 {
   const float s = std::sqrt(a);
   return ((double)s * (double)s < (double)a) ? std::nextafterf(s, INFINITY) : s;
+}
+GSQ_HD float sqrt_rd(float a)
+{
+  const float s = std::sqrt(a);
+  return ((double)s * (double)s > (double)a) ? std::nextafterf(s, -INFINITY) : s;
 }
 GSQ_HD float f_rn(double a) { return (float)a; }
 GSQ_HD float f_ru(double a)
@@ -454,6 +460,36 @@ GSQ_HD bool visit32_core(const float* lo_l, const float* hi_l, const float* lo_r
   return true;
 }
 
+
+// FP32 enclosure [lo2, hi2] of the FP64 squared distance the reference
+// computes between the query and an object point (squared_distance(Point,
+// Point), primal/operators/squared_distance.hpp:62-67), from the query
+// context (qf rounded to nearest, lip = 2^-21 (max|qf| + M)) and the object
+// point rounded to nearest (pf, |p| <= M).  With u = 2^-24: per coordinate
+// the rounded difference qf - pf is within u (max|qf| + M) of q - p, so
+// |q - p| is within sqrt(3) u (max|qf| + M) < lip / 4 of |qf - pf|; the FP32
+// offsets o = fl(qf - pf) are within u |o| of qf - pf and the fused dot d2 is
+// within 3.01 u of |o|^2, so |q - p| lies in sqrt(d2) (1 -+ 2.52 u) -+ lip / 4,
+// widened here to (1 -+ 4 u).  The FP64 evaluation rounds within 2^-50 of
+// |q - p|^2, covered by a further factor (1 -+ 2^-22).  Distances too small
+// for these FP32 bounds (or too large) give [0, inf): undecided.
+GSQ_HD void point_bounds32(const QCtx& c, const float* pf, float& lo2, float& hi2)
+{
+  const float o0 = c.qf[0] - pf[0], o1 = c.qf[1] - pf[1], o2 = c.qf[2] - pf[2];
+  const float d2 = dot3f(o0, o0, o1, o1, o2, o2);
+  const float e = fp::mul_ru(0.25f, c.lip);
+  const float slo = fp::sub_rd(fp::mul_rd(fp::sqrt_rd(d2), 1.f - 0x1p-22f), e);
+  const float shi = fp::add_ru(fp::mul_ru(fp::sqrt_ru(d2), 1.f + 0x1p-22f), e);
+  if(!(shi > 0x1p-60f && shi < 0x1p60f))
+  {
+    lo2 = 0.f;
+    hi2 = INFINITY;
+    return;
+  }
+  const float l = fmaxf(slo, 0.f);
+  lo2 = fp::mul_rd(fp::mul_rd(l, l), 1.f - 0x1p-22f);
+  hi2 = fp::mul_ru(fp::mul_ru(shi, shi), 1.f + 0x1p-22f);
+}
 
 // One child box of an FP64 node record as the FP32 node records hold it
 // (k_nodes32): lo rounded down, hi rounded up, and the returned slack (the

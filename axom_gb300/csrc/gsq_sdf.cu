@@ -76,6 +76,12 @@ __global__ void k_cell_boxes(const double* __restrict__ x, const double* __restr
   const int c = blockIdx.x * blockDim.x + threadIdx.x;
   if(c >= ncells) return;
   double lo[3] = {DBL_MAX, DBL_MAX, DBL_MAX}, hi[3] = {-DBL_MAX, -DBL_MAX, -DBL_MAX};
+  OKey klo[3], khi[3];
+  for(int d = 0; d < 3; ++d)
+  {
+    klo[d] = okey(lo[d]);
+    khi[d] = okey(hi[d]);
+  }
   for(int k = 0; k < npc; ++k)
   {
     int v = cells[(size_t)c * npc + k];
@@ -87,8 +93,17 @@ __global__ void k_cell_boxes(const double* __restrict__ x, const double* __restr
     const double p[3] = {x[v], y[v], z[v]};
     for(int d = 0; d < 3; ++d)
     {
-      if(p[d] < lo[d]) lo[d] = p[d];
-      if(p[d] > hi[d]) hi[d] = p[d];
+      const OKey kp = okey(p[d]);  // addPoint's comparisons on the integer pipe
+      if(ok_lt(kp, klo[d]))
+      {
+        lo[d] = p[d];
+        klo[d] = kp;
+      }
+      if(ok_gt(kp, khi[d]))
+      {
+        hi[d] = p[d];
+        khi[d] = kp;
+      }
     }
   }
   for(int d = 0; d < 3; ++d)

@@ -101,10 +101,15 @@ def test_build_edge_cases_match_oracle(gsq, port):
     zeros[::2] = -0.0
     zeros[1::4, 3:] = 1.0
     allinv = np.tile(np.array([[1.0, 1, 1, 0, 0, 0]]), (10, 1))
-    for boxes in (dup, inval, degen, zeros, allinv, np.concatenate([dup, inval, degen, zeros])):
+    nans = W.random_boxes(3000, 4)
+    nans[::5, 1] = np.nan  # still valid for BoundingBox::isValid, which compares with ">"
+    nans[2::5, 3] = np.nan
+    nans[3::5, [0, 3]] = np.nan
+    for boxes in (dup, inval, degen, zeros, allinv, nans, np.concatenate([dup, inval, degen, zeros, nans])):
         for scale in (1.000123, 1.0):
             b, h = check_layout(gsq, port, boxes, scale)
             q = np.concatenate([boxes[:200], W.random_boxes(200, 9) * 2 - 1])
+            q[::7, 4] = np.nan
             for x, y in zip(b.find_bounding_boxes(q), port.find_boxes(h, q)):
                 assert_bits_equal(x, y, "find boxes")
 
@@ -113,11 +118,14 @@ def test_find_points_and_rays_match_oracle(gsq, port):
     boxes = W.random_boxes(20000, 8)
     b, h = check_layout(gsq, port, boxes, 1.000123)
     p = W.rng(4).uniform(0, 1, (20000, 3))
+    p[::11, 2] = np.nan
     for x, y in zip(b.find_points(p), port.find_points(h, p)):
         assert_bits_equal(x, y, "find points")
     o = W.rng(5).uniform(-0.5, 1.5, (3000, 3))
     d = port.normalize_rays(W.rng(6).normal(size=(3000, 3)))
     d[::5, 1] = 0.0
+    o[::13, 0] = np.nan
+    d[::17, 2] = np.nan
     for x, y in zip(b.find_rays(o, d), port.find_rays(h, o, d)):
         assert_bits_equal(x, y, "find rays")
 

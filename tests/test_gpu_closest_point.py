@@ -61,3 +61,26 @@ def test_closest_point_device_arrays(gsq, port):
     idx, dom, pos, dist = cp.compute_closest_points(torch.from_numpy(q).cuda())
     want = port.cp_query(port.cp(pts), q, threads=8)
     check((idx.cpu().numpy(), dom.cpu().numpy(), pos.cpu().numpy(), dist.cpu().numpy()), want)
+
+
+def test_closest_point_ties_at_scale(gsq, port):
+    """The 655,362 vertices of the level-8 mesh as object points; 2M queries:
+    uniform in the 1.2x box, and at midpoints of mesh edges (two object points
+    at equal distance up to rounding, so the strict "closer" test and the
+    first-found rule decide).  Mixed against FP64 over every output, and a
+    sample against the oracle, bit for bit."""
+    import torch
+    from axom_gb300 import workloads as W
+    v, f = W.displaced_icosphere(8, 1234)
+    r = np.random.default_rng(12)
+    e = f[r.integers(0, f.shape[0], 1 << 20), :2]
+    q = np.concatenate([W.uniform_queries(v, 1 << 20, 13), 0.5 * (v[e[:, 0]] + v[e[:, 1]])])
+    qd = torch.from_numpy(q).cuda()
+    cp = gsq.ClosestPoint(v)
+    mixed = cp.compute_closest_points(qd, precision=axom_gb300.PRECISION_MIXED)
+    fp64 = cp.compute_closest_points(qd, precision=axom_gb300.PRECISION_FP64)
+    for x, y, what in zip(mixed, fp64, ("index", "domain", "position", "distance")):
+        assert_bits_equal(x.cpu().numpy(), y.cpu().numpy(), what)
+    idx = np.concatenate([np.arange(0, 1 << 20, 97), (1 << 20) + np.arange(0, 1 << 20, 97)])
+    want = port.cp_query(port.cp(v), q[idx], threads=16)
+    check(tuple(x.cpu().numpy()[idx] for x in mixed), want)

@@ -215,13 +215,18 @@ def test_port_matches_reference_edge_cases(port, ref):
     zeros = np.zeros((8, 6))
     zeros[::2] = -0.0
     zeros[1::4, 3:] = 1.0
-    for boxes in (dup, inval, degen, zeros, np.concatenate([dup, inval, degen, zeros])):
+    nans = W.random_boxes(40, 4)
+    nans[::5, 1] = np.nan  # a NaN coordinate: BoundingBox::isValid compares with ">", so still valid
+    nans[2::5, 3] = np.nan
+    nans[3::5, [0, 3]] = np.nan
+    for boxes in (dup, inval, degen, zeros, nans, np.concatenate([dup, inval, degen, zeros, nans])):
         for scale in (1.000123, 1.0):
             a, b = port.internals(boxes, scale), ref.internals(boxes, scale)
             for k in a:
                 assert_bits_equal(a[k], b[k], k)
             hp, hr = port.bvh(boxes, scale), ref.bvh(boxes, scale)
             q = np.concatenate([boxes[:20], W.random_boxes(20, 9) * 2 - 1])
+            q[::7, 4] = np.nan
             for x, y in zip(port.find_boxes(hp, q), ref.find_boxes(hr, q)):
                 assert_bits_equal(x, y, "find boxes")
 
