@@ -100,6 +100,7 @@ __global__ void __launch_bounds__(BT) k_b_mesh_bounds(const double* __restrict__
     const double p[3] = {x[v], y[v], z[v]};
     for(int d = 0; d < 3; ++d)
     {
+      if(okey(p[d]).nan) continue;  // addPoint's comparisons are false for a NaN
       lbvh::take_min(fv.lo[d], lbvh::ArgV {p[d], (int)v});
       lbvh::take_max(fv.hi[d], lbvh::ArgV {p[d], (int)v});
     }

@@ -123,15 +123,24 @@ __device__ __forceinline__ bool scale_box(double* lo, double* hi, double half)
   return valid;
 }
 
-// One valid scaled box into the bounds fold (reduce, SEQ branch, BR:134-141:
-// addBox from an invalid box = per-axis leftmost min of lo and leftmost max of
-// "lo if lo == hi else hi", the first valid box contributing its own hi).
+// One valid scaled box into the bounds fold.  reduce's SEQ branch (BR:134-141)
+// copies the first valid box and then, for every later valid box, calls
+// addPoint(lo) and addPoint(hi): per axis, strict "<" / ">" updates in that
+// order.  So a later box offers the min fold lo (or hi where lo is NaN) and
+// the max fold hi (lo where they are equal, so that the earlier of two equal
+// values, e.g. -0 before +0, is kept, or where hi is NaN); a NaN never wins a
+// comparison and is not offered.  The first valid box's own coordinates are
+// applied by bounds_params, a NaN among them included (a NaN copied into the
+// running box is never replaced).
 __device__ __forceinline__ void fold_add_box(Fold& f, const double* lo, const double* hi, int i)
 {
   for(int d = 0; d < 3; ++d)
   {
-    take_min(f.lo[d], ArgV {lo[d], i});
-    take_max(f.hi[d], ArgV {ok_eq(okey(lo[d]), okey(hi[d])) ? lo[d] : hi[d], i});
+    const OKey kl = okey(lo[d]), kh = okey(hi[d]);
+    const double vmin = kl.nan ? hi[d] : lo[d];
+    const double vmax = kl.nan ? hi[d] : (kh.nan ? lo[d] : (ok_eq(kl, kh) ? lo[d] : hi[d]));
+    if(!okey(vmin).nan) take_min(f.lo[d], ArgV {vmin, i});
+    if(!okey(vmax).nan) take_max(f.hi[d], ArgV {vmax, i});
   }
   f.first_valid = min(f.first_valid, i);
 }
@@ -154,10 +163,14 @@ __device__ __forceinline__ void bounds_params(const Fold& a, const double* __res
   }
   else
   {
+    // the first valid box's coordinates start the running box: they stand
+    // where they win (ties included, being first) and where they are NaN
+    const double* fb = leaf + 6 * (size_t)a.first_valid;
     for(int d = 0; d < 3; ++d)
     {
-      lo[d] = a.lo[d].v;
-      hi[d] = (a.hi[d].i == a.first_valid) ? leaf[6 * (size_t)a.first_valid + 3 + d] : a.hi[d].v;
+      const bool lnan = okey(fb[d]).nan, hnan = okey(fb[3 + d]).nan;
+      lo[d] = (lnan || a.lo[d].i == INT_MAX) ? fb[d] : a.lo[d].v;
+      hi[d] = (hnan || a.hi[d].i == INT_MAX || a.hi[d].i == a.first_valid) ? fb[3 + d] : a.hi[d].v;
     }
   }
   for(int d = 0; d < 3; ++d)

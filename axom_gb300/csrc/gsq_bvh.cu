@@ -375,6 +375,7 @@ __global__ void __launch_bounds__(BUILD_THREADS) k_node_fold(const double* __res
     const double p[3] = {x[i], y[i], z[i]};
     for(int d = 0; d < 3; ++d)
     {
+      if(okey(p[d]).nan) continue;  // addPoint's comparisons are false for a NaN
       take_min(f.lo[d], ArgV {p[d], i});
       take_max(f.hi[d], ArgV {p[d], i});
     }
