@@ -108,6 +108,11 @@ __global__ void k_cpq_codes(const double* __restrict__ q, int m, const double* b
 }
 
 // The point traverser's FP64 node step with the closest-point predicate.
+// KEYS: the comparisons on the integer pipe (OKey, the FP64 outcomes), for the
+// one-thread-per-query FP64 kernel, which the FP64 pipe bounds; the persistent
+// kernel runs this step only in converged batches and keeps FP64 comparisons,
+// which need fewer registers.
+template <bool KEYS>
 __device__ __forceinline__ void cpq_visit_fp64(const NodeRec64* __restrict__ nodes, int cur, const double* q,
                                                double best, double thr, bool& inL, bool& inR, bool& swap)
 {
@@ -122,22 +127,35 @@ __device__ __forceinline__ void cpq_visit_fp64(const NodeRec64* __restrict__ nod
   }
   inL = false;
   inR = false;
-  if(box_valid(b, b + 3))
+  for(int side = 0; side < 2; ++side)
   {
-    const double sq = sqdist_pb(q, b, b + 3);
-    inL = sq <= best && sq <= thr;
-  }
-  if(box_valid(b + 6, b + 9))
-  {
-    const double sq = sqdist_pb(q, b + 6, b + 9);
-    inR = sq <= best && sq <= thr;
+    const double* lo = b + 6 * side;
+    const double* hi = lo + 3;
+    bool in = false;
+    if constexpr(KEYS)
+    {
+      if(box_valid_i(lo, hi))
+      {
+        const OKey ks = okey(sqdist_pb(q, lo, hi));
+        in = ok_le(ks, okey(best)) && ok_le(ks, okey(thr));
+      }
+    }
+    else if(box_valid(lo, hi))
+    {
+      const double sq = sqdist_pb_d(q, lo, hi);
+      in = sq <= best && sq <= thr;
+    }
+    (side ? inR : inL) = in;
   }
   swap = false;
   if(inL && inR)
   {
     const double cl[3] = {0.5 * (b[0] + b[3]), 0.5 * (b[1] + b[4]), 0.5 * (b[2] + b[5])};
     const double cr[3] = {0.5 * (b[6] + b[9]), 0.5 * (b[7] + b[10]), 0.5 * (b[8] + b[11])};
-    swap = sqdist_pp(q, cl) > sqdist_pp(q, cr);
+    if constexpr(KEYS)
+      swap = ok_gt(okey(sqdist_pp(q, cl)), okey(sqdist_pp(q, cr)));
+    else
+      swap = sqdist_pp(q, cl) > sqdist_pp(q, cr);
   }
 }
 
@@ -162,13 +180,13 @@ __global__ void __launch_bounds__(128) k_cpq(const NodeRec64* __restrict__ nodes
   int bleaf = -1;
   auto visit = [&](int cur, bool& inL, bool& inR, bool& swap, int2& ch) {
     ch = __ldg(reinterpret_cast<const int2*>(nodes64[cur].child));
-    cpq_visit_fp64(nodes64, cur, q, best, thr, inL, inR, swap);
+    cpq_visit_fp64<true>(nodes64, cur, q, best, thr, inL, inR, swap);
   };
   auto leaf = [&](int leafpos) {
     const PointRec r = recs[leafpos];
     if(r.id < 0) return;
     const double sq = sqdist_pp(q, r.p);
-    if(sq < best)
+    if(ok_lt(okey(sq), okey(best)))
     {
       best = sq;
       bleaf = leafpos;
@@ -360,7 +378,7 @@ __global__ void __launch_bounds__(128) k_cpq_persist(const NodeRec64* __restrict
       if(p == P_NODE)
       {
         bool inL, inR, swap;
-        cpq_visit_fp64(nodes64, cur, q, best, thr, inL, inR, swap);
+        cpq_visit_fp64<false>(nodes64, cur, q, best, thr, inL, inR, swap);
         apply_visit(inL, inR, swap, pch);
       }
       else if(p == P_FINISH)

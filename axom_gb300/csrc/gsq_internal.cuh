@@ -234,43 +234,96 @@ __host__ __device__ inline bool box_valid(const double* lo, const double* hi)
 
 // ---- exact FP64 comparisons on the integer pipe ----------------------------
 // This GPU executes FP64 instructions, comparisons included, at a small
-// fraction of its FP32/integer rate, so comparison-heavy loops (box tests,
-// addBox, the bounds fold) compare doubles through their bit patterns: for
-// non-NaN x, y the map  k(x) = b ^ ((b >> 63) & INT64_MAX)  (b the bits, with
-// -0 taken as +0) is strictly increasing, so x < y exactly when k(x) < k(y)
-// and x == y exactly when k(x) == k(y).  Any comparison involving a NaN is
-// false, as in IEEE arithmetic; the results equal the FP64 comparisons.
+// fraction of its FP32/integer rate (and its 64-bit integer operations share
+// that cost, as ncu's FP64-pipe counters show), so comparison-heavy loops (box
+// tests, addBox, the bounds fold, the closest-point region tests) compare
+// doubles through their bit patterns with 32-bit operations: for non-NaN x, y
+// with the 64 bits b (and -0 taken as +0), the map b -> b ^ ((b >> 63) &
+// INT64_MAX) is strictly increasing, so the keys' lexicographic order on
+// (signed high word, unsigned low word) is the FP64 order, and equal keys mean
+// equal values.  Any comparison involving a NaN is false, as in IEEE
+// arithmetic; the results equal the FP64 comparisons.
 struct OKey
 {
-  long long k;
+  int hi;
+  unsigned lo;
   bool nan;
 };
 
-__host__ __device__ inline long long dbits(double x)
+__host__ __device__ inline void dwords(double x, int& hi, unsigned& lo)
 {
 #ifdef __CUDA_ARCH__
-  return __double_as_longlong(x);
+  hi = __double2hiint(x);
+  lo = (unsigned)__double2loint(x);
 #else
-  long long b;
+  unsigned long long b;
   __builtin_memcpy(&b, &x, sizeof b);
-  return b;
+  hi = (int)(unsigned)(b >> 32);
+  lo = (unsigned)b;
 #endif
 }
 
 __host__ __device__ inline OKey okey(double x)
 {
-  long long b = dbits(x);
+  int h;
+  unsigned l;
+  dwords(x, h, l);
+  const int mag = h & 0x7FFFFFFF;
   OKey r;
-  r.nan = (b & 0x7FFFFFFFFFFFFFFFLL) > 0x7FF0000000000000LL;
-  if(b == (long long)0x8000000000000000ULL) b = 0;
-  r.k = b ^ ((b >> 63) & 0x7FFFFFFFFFFFFFFFLL);
+  r.nan = mag > 0x7FF00000 || (mag == 0x7FF00000 && l != 0u);
+  if(mag == 0 && l == 0u) h = 0;  // -0 as +0
+  if(h < 0)
+  {
+    h ^= 0x7FFFFFFF;
+    l = ~l;
+  }
+  r.hi = h;
+  r.lo = l;
   return r;
 }
-__host__ __device__ inline bool ok_lt(const OKey& a, const OKey& b) { return !(a.nan | b.nan) && a.k < b.k; }
-__host__ __device__ inline bool ok_gt(const OKey& a, const OKey& b) { return !(a.nan | b.nan) && a.k > b.k; }
-__host__ __device__ inline bool ok_le(const OKey& a, const OKey& b) { return !(a.nan | b.nan) && a.k <= b.k; }
-__host__ __device__ inline bool ok_ge(const OKey& a, const OKey& b) { return !(a.nan | b.nan) && a.k >= b.k; }
-__host__ __device__ inline bool ok_eq(const OKey& a, const OKey& b) { return !(a.nan | b.nan) && a.k == b.k; }
+__host__ __device__ inline bool ok_klt(const OKey& a, const OKey& b) { return a.hi < b.hi || (a.hi == b.hi && a.lo < b.lo); }
+__host__ __device__ inline bool ok_keq(const OKey& a, const OKey& b) { return a.hi == b.hi && a.lo == b.lo; }
+__host__ __device__ inline bool ok_lt(const OKey& a, const OKey& b) { return !(a.nan | b.nan) && ok_klt(a, b); }
+__host__ __device__ inline bool ok_gt(const OKey& a, const OKey& b) { return !(a.nan | b.nan) && ok_klt(b, a); }
+__host__ __device__ inline bool ok_le(const OKey& a, const OKey& b) { return !(a.nan | b.nan) && !ok_klt(b, a); }
+__host__ __device__ inline bool ok_ge(const OKey& a, const OKey& b) { return !(a.nan | b.nan) && !ok_klt(a, b); }
+__host__ __device__ inline bool ok_eq(const OKey& a, const OKey& b) { return !(a.nan | b.nan) && ok_keq(a, b); }
+
+// Comparisons with CP_EPS on the integer pipe, in 32-bit words (the FP64
+// pipe of this GPU is scarce): with (h, l) the signed high and unsigned low
+// words of x, x > EPS exactly when (h, l) lies in (EPS, INF] in lexicographic
+// order (negative values have h < 0; NaNs lie above INF or are negative),
+// x < -EPS exactly when h < 0 and the magnitude (h & INT32_MAX, l) lies in
+// (EPS, INF], and |x| <= EPS exactly when the magnitude is at most EPS.
+constexpr int CP_EPS_HI = 0x3D719799;           // the words of 1e-12
+constexpr unsigned CP_EPS_LO = 0x812DEA11u;
+__host__ __device__ inline bool mag_gt_eps(int m, unsigned l)
+{
+  return m > CP_EPS_HI || (m == CP_EPS_HI && l > CP_EPS_LO);
+}
+__host__ __device__ inline bool mag_le_inf(int m, unsigned l) { return m < 0x7FF00000 || (m == 0x7FF00000 && l == 0u); }
+__host__ __device__ inline bool gt_eps(double x)
+{
+  int h;
+  unsigned l;
+  dwords(x, h, l);
+  return h >= 0 && mag_gt_eps(h, l) && mag_le_inf(h, l);
+}
+__host__ __device__ inline bool lt_neg_eps(double x)
+{
+  int h;
+  unsigned l;
+  dwords(x, h, l);
+  const int m = h & 0x7FFFFFFF;
+  return h < 0 && mag_gt_eps(m, l) && mag_le_inf(m, l);
+}
+__host__ __device__ inline bool abs_le_eps(double x)
+{
+  int h;
+  unsigned l;
+  dwords(x, h, l);
+  return !mag_gt_eps(h & 0x7FFFFFFF, l);
+}
 
 // box_valid on keys
 __host__ __device__ inline bool box_valid_k(const OKey* lo, const OKey* hi)

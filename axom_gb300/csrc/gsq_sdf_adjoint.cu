@@ -56,7 +56,7 @@ __device__ __forceinline__ void closest_point_bary(const double* P, const double
     return;
   }
   const double vc = d1 * d4 - d3 * d2;
-  if(is_leq(vc, 0.0) && is_geq(d1, 0.0) && is_leq(d3, 0.0) && !near_eq(d1, d3, CP_EPS))
+  if(is_leq(vc, 0.0) && is_geq(d1, 0.0) && is_leq(d3, 0.0) && !abs_le_eps(d1 - d3))
   {
     const double v = d1 / (d1 - d3);
     out[0] = A[0] + ab0 * v, out[1] = A[1] + ab1 * v, out[2] = A[2] + ab2 * v;

@@ -37,14 +37,20 @@ __device__ __forceinline__ double sqdist_pp(const double* a, const double* b)
   return dot3(v0, v1, v2, v0, v1, v2);
 }
 
-__device__ __forceinline__ bool is_leq(double x, double y) { return !((x > y) && !near_eq(x, y, CP_EPS)); }
-__device__ __forceinline__ bool is_geq(double x, double y) { return !((x < y) && !near_eq(x, y, CP_EPS)); }
+__device__ __forceinline__ bool is_leq(double x, double y)
+{
+  return !(ok_gt(okey(x), okey(y)) && !abs_le_eps(x - y));
+}
+__device__ __forceinline__ bool is_geq(double x, double y)
+{
+  return !(ok_lt(okey(x), okey(y)) && !abs_le_eps(x - y));
+}
 // The same predicates in one comparison, given d = x - y rounded: x > y makes
 // the rounded difference positive (FP64 keeps subnormals), so "x > y and
 // |x - y| > EPS" is "d > EPS", and "x < y and |x - y| > EPS" is "d < -EPS";
 // NaNs give true as in is_leq/is_geq.  For y = 0, d is x itself.
-__device__ __forceinline__ bool leq_d(double d) { return !(d > CP_EPS); }
-__device__ __forceinline__ bool geq_d(double d) { return !(d < -CP_EPS); }
+__device__ __forceinline__ bool leq_d(double d) { return !gt_eps(d); }
+__device__ __forceinline__ bool geq_d(double d) { return !lt_neg_eps(d); }
 
 // closest_point(Point, Triangle, loc, EPS) (primal/operators/closest_point.hpp:162-290)
 __device__ __forceinline__ int closest_point(const double* P, const double* A, const double* B, const double* C,
@@ -69,7 +75,7 @@ __device__ __forceinline__ int closest_point(const double* P, const double* A, c
     return 1;
   }
   const double vc = d1 * d4 - d3 * d2;
-  if(leq_d(vc) && geq_d(d1) && leq_d(d3) && !near_eq(d1, d3, CP_EPS))
+  if(leq_d(vc) && geq_d(d1) && leq_d(d3) && !abs_le_eps(d1 - d3))
   {
     const double v = d1 / (d1 - d3);
     out[0] = A[0] + ab0 * v, out[1] = A[1] + ab1 * v, out[2] = A[2] + ab2 * v;
@@ -150,7 +156,7 @@ __device__ __forceinline__ bool tri_degenerate(const double* A, const double* B,
   double n[3];
   tri_normal(A, B, C, n);
   const double area = 0.5 * sqrt(dot3(n[0], n[1], n[2], n[0], n[1], n[2]));
-  return near_eq(area, 0.0, 1.0e-12);
+  return abs_le_eps(area);  // isNearlyEqual(area, 0, 1e-12)
 }
 
 // MinCandidate (SD:159-175); the closest element's geometry is kept as its
@@ -235,9 +241,9 @@ __device__ __forceinline__ void apply_candidate(const double* cp, double sq, int
   const int ty = (loc < 0) ? 1 : (loc <= 2) ? 0 : 2;
   const bool shared = (ty != 2);
   bool upd;
-  if(sq < m.minSq)
+  if(ok_lt(okey(sq), okey(m.minSq)))
   {
-    const bool clear = !shared || (m.type != ty) || !near_eq(sqdist_pp(cp, m.mp), 0.0, CP_EPS);
+    const bool clear = !shared || (m.type != ty) || !abs_le_eps(sqdist_pp(cp, m.mp));
     m.minSq = sq;
     m.mp[0] = cp[0], m.mp[1] = cp[1], m.mp[2] = cp[2];
     m.type = ty;
@@ -251,7 +257,7 @@ __device__ __forceinline__ void apply_candidate(const double* cp, double sq, int
     upd = computeNormal && shared;
   }
   else
-    upd = computeNormal && shared && (m.type == ty) && near_eq(sqdist_pp(cp, m.mp), 0.0, CP_EPS);
+    upd = computeNormal && shared && (m.type == ty) && abs_le_eps(sqdist_pp(cp, m.mp));
   if(upd)
   {
     if(m.npend == NPEND) flush_normals<NPC>(m, leaves);
@@ -272,7 +278,34 @@ __device__ __forceinline__ void check_triangle(const double* q, MinCand& m, cons
 }
 
 // squared_distance(Point, BoundingBox) (squared_distance.hpp:77-102)
+// (its comparisons on the integer pipe, OKey, with the FP64 outcomes; keys
+// are formed one axis at a time, so that few stay live)
+__device__ __forceinline__ bool box_valid_i(const double* lo, const double* hi)
+{
+  bool ok = true;
+#pragma unroll
+  for(int d = 0; d < 3; ++d) ok = ok && !ok_gt(okey(lo[d]), okey(hi[d]));
+  return ok;
+}
 __device__ __forceinline__ double sqdist_pb(const double* p, const double* lo, const double* hi)
+{
+  if(!box_valid_i(lo, hi)) return DBL_MAX;
+  bool out = false;
+  double c[3];
+#pragma unroll
+  for(int d = 0; d < 3; ++d)
+  {
+    const OKey kp = okey(p[d]);
+    const bool below = ok_lt(kp, okey(lo[d])), above = ok_gt(kp, okey(hi[d]));
+    out = out || below || above;
+    c[d] = below ? lo[d] : above ? hi[d] : p[d];
+  }
+  if(!out) return 0.0;
+  return sqdist_pp(p, c);
+}
+// The same with FP64 comparisons (fewer registers), for code that runs only
+// in converged FP64 batches.
+__device__ __forceinline__ double sqdist_pb_d(const double* p, const double* lo, const double* hi)
 {
   if(!box_valid(lo, hi)) return DBL_MAX;
   if(!(p[0] < lo[0] || p[0] > hi[0] || p[1] < lo[1] || p[1] > hi[1] || p[2] < lo[2] || p[2] > hi[2])) return 0.0;
@@ -432,14 +465,14 @@ __device__ __forceinline__ void visit_fp64(const NodeRec64* __restrict__ nodes, 
     b[2 * k] = t.x;
     b[2 * k + 1] = t.y;
   }
-  inL = box_valid(b, b + 3) ? (sqdist_pb(q, b, b + 3) <= minSq) : false;
-  inR = box_valid(b + 6, b + 9) ? (sqdist_pb(q, b + 6, b + 9) <= minSq) : false;
+  inL = box_valid_i(b, b + 3) ? ok_le(okey(sqdist_pb(q, b, b + 3)), okey(minSq)) : false;
+  inR = box_valid_i(b + 6, b + 9) ? ok_le(okey(sqdist_pb(q, b + 6, b + 9)), okey(minSq)) : false;
   swap = false;
   if(inL && inR)
   {
     const double cl[3] = {0.5 * (b[0] + b[3]), 0.5 * (b[1] + b[4]), 0.5 * (b[2] + b[5])};
     const double cr[3] = {0.5 * (b[6] + b[9]), 0.5 * (b[7] + b[10]), 0.5 * (b[8] + b[11])};
-    swap = sqdist_pp(q, cl) > sqdist_pp(q, cr);
+    swap = ok_gt(okey(sqdist_pp(q, cl)), okey(sqdist_pp(q, cr)));
   }
 }
 
