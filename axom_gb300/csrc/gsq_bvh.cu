@@ -26,6 +26,7 @@
 #include <climits>
 #include <cstdlib>
 #include <cstring>
+#include <mutex>
 #include <vector>
 
 using namespace gsq;
@@ -637,6 +638,33 @@ int bvh_build(BvhDev& B, const double* d_boxes, int n, double scale, cudaStream_
 // =============================================================================
 // C ABI: spin::BVH
 // =============================================================================
+// What a find needs besides its inputs and outputs, kept with the handle so
+// that a find allocates only its candidate array: the pass-1 candidate
+// scratch, the scan's tile sums and the device total (grow-only), the timing
+// events, and a pinned host word pair into which the total and the device
+// error word are read back together.  The reference's find* are const and
+// may run concurrently; a find that finds the cache in use by another thread
+// allocates its own scratch for the call instead.
+struct FindCache
+{
+  std::mutex busy;
+  void* work = nullptr;
+  size_t work_bytes = 0;
+  long long* host = nullptr;  // pinned: [0] total, [1] error word
+  cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
+  void release()
+  {
+    if(work) cudaFree(work);
+    if(host) cudaFreeHost(host);
+    for(auto& e : ev)
+      if(e) cudaEventDestroy(e);
+    work = nullptr;
+    host = nullptr;
+    work_bytes = 0;
+    for(auto& e : ev) e = nullptr;
+  }
+};
+
 struct gsq_bvh
 {
   int device = 0;
@@ -646,6 +674,7 @@ struct gsq_bvh
   bool built = false;
   float build_ms = 0.f;
   mutable float find_ms = 0.f;  // device time of the last find's two passes and scan
+  mutable FindCache fc;
   int* d_err = nullptr;
 };
 
@@ -676,40 +705,81 @@ int find_impl(const gsq_bvh* h, const double* a, const double* b, int32_t m, int
   OutBuf off_buf, cnt_buf;
   GSQ_CUDA_TRY(off_buf.prepare(offsets, sizeof(int) * (size_t)m, s));
   GSQ_CUDA_TRY(cnt_buf.prepare(counts, sizeof(int) * (size_t)m, s));
-  Scratch keep, tot;
-  GSQ_CUDA_TRY(keep.alloc(sizeof(int) * FIND_CAP * (size_t)std::max(m, 1), s));
-  GSQ_CUDA_TRY(tot.alloc(sizeof(long long), s));
+  // scratch: the handle's cache, or (when another thread holds it) the call's own
+  const size_t keep_bytes = (sizeof(int) * FIND_CAP * (size_t)std::max(m, 1) + 255) & ~size_t(255);
+  const size_t scan_bytes = (exclusive_scan_work_bytes(m) + 255) & ~size_t(255);
+  const size_t need = keep_bytes + scan_bytes + 256;
+  FindCache& fc = h->fc;
+  std::unique_lock<std::mutex> lock(fc.busy, std::try_to_lock);
+  const bool cached = lock.owns_lock();
+  Scratch own;
+  Events own_ev;
+  long long own_host[2];
+  char* work = nullptr;
+  cudaEvent_t* ev = nullptr;
+  long long* hostw = own_host;
+  if(cached)
+  {
+    if(need > fc.work_bytes)
+    {
+      if(fc.work) cudaFree(fc.work);
+      fc.work = nullptr;
+      fc.work_bytes = 0;
+      GSQ_CUDA_TRY(cudaMalloc(&fc.work, need));
+      fc.work_bytes = need;
+    }
+    if(!fc.host) GSQ_CUDA_TRY(cudaMallocHost(&fc.host, 2 * sizeof(long long)));
+    for(auto& e : fc.ev)
+      if(!e) GSQ_CUDA_TRY(cudaEventCreate(&e));
+    work = static_cast<char*>(fc.work);
+    ev = fc.ev;
+    hostw = fc.host;
+  }
+  else
+  {
+    GSQ_CUDA_TRY(own.alloc(need, s));
+    GSQ_CUDA_TRY(own_ev.create());
+    work = own.as<char>();
+    ev = own_ev.e;
+  }
+  int* keep = reinterpret_cast<int*>(work);
+  void* scan_work = work + keep_bytes;
+  long long* d_tot = reinterpret_cast<long long*>(work + keep_bytes + scan_bytes);
   QueryArgs qa {static_cast<const double*>(qa_buf.dev), static_cast<const double*>(qb_buf.dev), h->tol};
   int* d_cnt = static_cast<int*>(cnt_buf.dev);
   int* d_off = static_cast<int*>(off_buf.dev);
-  Events ev;
-  GSQ_CUDA_TRY(ev.create());
-  cudaEventRecord(ev.e[0], s);
+  cudaEventRecord(ev[0], s);
   if(m > 0)
   {
     count_launch();
     k_find_pass1<KIND><<<grid_for(m, FIND_THREADS), FIND_THREADS, 0, s>>>(h->dev.nodes, h->dev.perm, qa, m, d_cnt,
-                                                                          keep.as<int>(), h->d_err);
+                                                                          keep, h->d_err);
   }
-  rc = exclusive_scan(d_cnt, d_off, m, tot.as<long long>(), s);
+  rc = exclusive_scan(d_cnt, d_off, m, d_tot, s, scan_work);
   if(rc) return rc;
-  cudaEventRecord(ev.e[1], s);
-  long long total = 0;
-  GSQ_CUDA_TRY(cudaMemcpyAsync(&total, tot.p, sizeof(long long), cudaMemcpyDeviceToHost, s));
+  cudaEventRecord(ev[1], s);
+  // the total and the device error word in one read-back
+  hostw[1] = 0;
+  GSQ_CUDA_TRY(cudaMemcpyAsync(hostw, d_tot, sizeof(long long), cudaMemcpyDeviceToHost, s));
+  GSQ_CUDA_TRY(cudaMemcpyAsync(hostw + 1, h->d_err, sizeof(int), cudaMemcpyDeviceToHost, s));
   GSQ_CUDA_TRY(cudaStreamSynchronize(s));
-  rc = check_device_error(h->d_err, s, "find pass 1");
-  if(rc) return rc;
+  const long long total = hostw[0];
+  if(static_cast<int>(hostw[1]) != 0)
+  {
+    rc = check_device_error(h->d_err, s, "find pass 1");  // reports and clears the word
+    if(rc) return rc;
+  }
   if(total > INT_MAX) return fail(GSQ_ERR_INVALID, "more than 2^31-1 candidates");
   int* d_cand = nullptr;
   GSQ_CUDA_TRY(cudaMalloc(&d_cand, sizeof(int) * (size_t)std::max<long long>(total, 1)));
-  cudaEventRecord(ev.e[2], s);
+  cudaEventRecord(ev[2], s);
   if(m > 0)
   {
     count_launch();
     k_find_pass2<KIND><<<grid_for(m, FIND_THREADS), FIND_THREADS, 0, s>>>(h->dev.nodes, h->dev.perm, qa, m, d_cnt,
-                                                                          d_off, keep.as<int>(), d_cand);
+                                                                          d_off, keep, d_cand);
   }
-  cudaEventRecord(ev.e[3], s);
+  cudaEventRecord(ev[3], s);
   cudaError_t e = cudaGetLastError();
   if(e == cudaSuccess) e = off_buf.flush(s);
   if(e == cudaSuccess) e = cnt_buf.flush(s);
@@ -743,8 +813,8 @@ int find_impl(const gsq_bvh* h, const double* a, const double* b, int32_t m, int
   }
   if(total_out) *total_out = total;
   float t01 = 0.f, t23 = 0.f;
-  cudaEventElapsedTime(&t01, ev.e[0], ev.e[1]);
-  cudaEventElapsedTime(&t23, ev.e[2], ev.e[3]);
+  cudaEventElapsedTime(&t01, ev[0], ev[1]);
+  cudaEventElapsedTime(&t23, ev[2], ev[3]);
   h->find_ms = t01 + t23;
   return GSQ_OK;
 }
@@ -773,6 +843,7 @@ int gsq_bvh_destroy(gsq_bvh* h)
 {
   if(!h) return GSQ_OK;
   h->dev.release();
+  h->fc.release();
   if(h->d_err) cudaFree(h->d_err);
   delete h;
   return GSQ_OK;

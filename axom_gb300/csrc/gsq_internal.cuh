@@ -215,7 +215,10 @@ int radix_sort_pairs_prealloc(uint32_t* keys[2], int* vals[2], int n, int end_bi
 
 // Exclusive scan of m int32 counts into offsets; *d_total (device int64)
 // receives the sum.
-int exclusive_scan(const int* d_in, int* d_out, int m, long long* d_total, cudaStream_t s);
+// work: exclusive_scan_work_bytes(m) bytes of device scratch, or null to
+// allocate it for the call.
+int exclusive_scan(const int* d_in, int* d_out, int m, long long* d_total, cudaStream_t s, void* work = nullptr);
+size_t exclusive_scan_work_bytes(int m);
 
 // Reads and clears the device error word; returns a GSQ status.
 int check_device_error(int* d_err, cudaStream_t s, const char* what);

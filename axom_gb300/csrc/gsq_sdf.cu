@@ -461,9 +461,20 @@ int gsq_sdf_eval(const gsq_sdf* hc, const double* qx, const double* qy, const do
   cudaEventRecord(e0, s);
   if(mixed)
   {
+    // the persistent kernel's work counter: the handle's, or the call's own
+    // when another thread is evaluating on this handle (computeDistances is
+    // const and re-entrant)
+    std::unique_lock<std::mutex> lock(h->work_busy, std::try_to_lock);
+    Scratch own_work;
+    int* work = h->d_work;
+    if(!lock.owns_lock())
+    {
+      GSQ_CUDA_TRY(own_work.alloc(sizeof(int), s));
+      work = own_work.as<int>();
+    }
     rc = mixed_launch(h->npc, B->nodes, h->nodes32, h->leaves, h->leaves32, h->d_mesh, qp, m, order, prm,
                       static_cast<double*>(ob.dev), static_cast<double*>(cb.dev), static_cast<double*>(nb.dev),
-                      h->d_err, audit ? h->d_audit : nullptr, h->d_work, h->opts.block_size, h->opts.queue_depth, s);
+                      h->d_err, audit ? h->d_audit : nullptr, work, h->opts.block_size, h->opts.queue_depth, s);
     if(rc) return rc;
   }
   else

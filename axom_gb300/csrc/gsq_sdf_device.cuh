@@ -49,10 +49,28 @@ __device__ __forceinline__ bool is_geq(double x, double y)
 // the rounded difference positive (FP64 keeps subnormals), so "x > y and
 // |x - y| > EPS" is "d > EPS", and "x < y and |x - y| > EPS" is "d < -EPS";
 // NaNs give true as in is_leq/is_geq.  For y = 0, d is x itself.
-__device__ __forceinline__ bool leq_d(double d) { return !gt_eps(d); }
-__device__ __forceinline__ bool geq_d(double d) { return !lt_neg_eps(d); }
+// KEYS: the comparison on the integer pipe (for the FP64-pipe-bound
+// one-thread-per-point kernels) or as an FP64 comparison (for the mixed
+// kernels' converged FP64 batches, where the integer form measured slower).
+template <bool KEYS = true>
+__device__ __forceinline__ bool leq_d(double d)
+{
+  if constexpr(KEYS)
+    return !gt_eps(d);
+  else
+    return !(d > CP_EPS);
+}
+template <bool KEYS = true>
+__device__ __forceinline__ bool geq_d(double d)
+{
+  if constexpr(KEYS)
+    return !lt_neg_eps(d);
+  else
+    return !(d < -CP_EPS);
+}
 
 // closest_point(Point, Triangle, loc, EPS) (primal/operators/closest_point.hpp:162-290)
+template <bool KEYS = true>
 __device__ __forceinline__ int closest_point(const double* P, const double* A, const double* B, const double* C,
                                              double* out)
 {
@@ -61,7 +79,7 @@ __device__ __forceinline__ int closest_point(const double* P, const double* A, c
   const double ap0 = P[0] - A[0], ap1 = P[1] - A[1], ap2 = P[2] - A[2];
   const double d1 = dot3(ab0, ab1, ab2, ap0, ap1, ap2);
   const double d2 = dot3(ac0, ac1, ac2, ap0, ap1, ap2);
-  if(leq_d(d1) && leq_d(d2))  // is_leq(d1, 0) && is_leq(d2, 0)
+  if(leq_d<KEYS>(d1) && leq_d<KEYS>(d2))  // is_leq(d1, 0) && is_leq(d2, 0)
   {
     out[0] = A[0], out[1] = A[1], out[2] = A[2];
     return 0;
@@ -69,13 +87,13 @@ __device__ __forceinline__ int closest_point(const double* P, const double* A, c
   const double bp0 = P[0] - B[0], bp1 = P[1] - B[1], bp2 = P[2] - B[2];
   const double d3 = dot3(ab0, ab1, ab2, bp0, bp1, bp2);
   const double d4 = dot3(ac0, ac1, ac2, bp0, bp1, bp2);
-  if(geq_d(d3) && leq_d(d4 - d3))  // is_geq(d3, 0) && is_leq(d4, d3)
+  if(geq_d<KEYS>(d3) && leq_d<KEYS>(d4 - d3))  // is_geq(d3, 0) && is_leq(d4, d3)
   {
     out[0] = B[0], out[1] = B[1], out[2] = B[2];
     return 1;
   }
   const double vc = d1 * d4 - d3 * d2;
-  if(leq_d(vc) && geq_d(d1) && leq_d(d3) && !abs_le_eps(d1 - d3))
+  if(leq_d<KEYS>(vc) && geq_d<KEYS>(d1) && leq_d<KEYS>(d3) && !abs_le_eps(d1 - d3))
   {
     const double v = d1 / (d1 - d3);
     out[0] = A[0] + ab0 * v, out[1] = A[1] + ab1 * v, out[2] = A[2] + ab2 * v;
@@ -84,20 +102,20 @@ __device__ __forceinline__ int closest_point(const double* P, const double* A, c
   const double cp0 = P[0] - C[0], cp1 = P[1] - C[1], cp2 = P[2] - C[2];
   const double d5 = dot3(ab0, ab1, ab2, cp0, cp1, cp2);
   const double d6 = dot3(ac0, ac1, ac2, cp0, cp1, cp2);
-  if(geq_d(d6) && leq_d(d5 - d6))  // is_geq(d6, 0) && is_leq(d5, d6)
+  if(geq_d<KEYS>(d6) && leq_d<KEYS>(d5 - d6))  // is_geq(d6, 0) && is_leq(d5, d6)
   {
     out[0] = C[0], out[1] = C[1], out[2] = C[2];
     return 2;
   }
   const double vb = d5 * d2 - d1 * d6;
-  if(leq_d(vb) && geq_d(d2) && leq_d(d6))
+  if(leq_d<KEYS>(vb) && geq_d<KEYS>(d2) && leq_d<KEYS>(d6))
   {
     const double w = d2 / (d2 - d6);
     out[0] = A[0] + ac0 * w, out[1] = A[1] + ac1 * w, out[2] = A[2] + ac2 * w;
     return -3;
   }
   const double va = d3 * d6 - d5 * d4;
-  if(leq_d(va) && geq_d(d4 - d3) && geq_d(d5 - d6))
+  if(leq_d<KEYS>(va) && geq_d<KEYS>(d4 - d3) && geq_d<KEYS>(d5 - d6))
   {
     const double w = (d4 - d3) / ((d4 - d3) + (d5 - d6));
     out[0] = B[0] + (C[0] - B[0]) * w, out[1] = B[1] + (C[1] - B[1]) * w, out[2] = B[2] + (C[2] - B[2]) * w;
@@ -267,13 +285,13 @@ __device__ __forceinline__ void apply_candidate(const double* cp, double sq, int
 
 // checkCandidate for one triangle (SD:667-736); sub-triangle `sub` of leaf
 // `leafpos` with vertices T.
-template <int NPC>
+template <int NPC, bool KEYS = true>
 __device__ __forceinline__ void check_triangle(const double* q, MinCand& m, const double* const* T,
                                                const LeafRec<NPC>* __restrict__ leaves, int leafpos, int sub,
                                                bool computeNormal)
 {
   double cp[3];
-  const int loc = closest_point(q, T[0], T[1], T[2], cp);
+  const int loc = closest_point<KEYS>(q, T[0], T[1], T[2], cp);
   apply_candidate<NPC>(cp, sqdist_pp(q, cp), loc, m, leaves, leafpos, sub, computeNormal);
 }
 
@@ -452,6 +470,7 @@ __device__ __forceinline__ void check_leaf(const double* q, MinCand& mc, const L
 // One node visit of the point traverser in FP64 (bvh_traverse.hpp:93-99 with
 // the traversePref of policy/LinearBVH.hpp:75-82): child predicates and, when
 // both children pass, whether to swap.
+template <bool KEYS = true>
 __device__ __forceinline__ void visit_fp64(const NodeRec64* __restrict__ nodes, int cur, const double* q, double minSq,
                                            bool& inL, bool& inR, bool& swap)
 {
@@ -465,14 +484,25 @@ __device__ __forceinline__ void visit_fp64(const NodeRec64* __restrict__ nodes, 
     b[2 * k] = t.x;
     b[2 * k + 1] = t.y;
   }
-  inL = box_valid_i(b, b + 3) ? ok_le(okey(sqdist_pb(q, b, b + 3)), okey(minSq)) : false;
-  inR = box_valid_i(b + 6, b + 9) ? ok_le(okey(sqdist_pb(q, b + 6, b + 9)), okey(minSq)) : false;
+  if constexpr(KEYS)
+  {
+    inL = box_valid_i(b, b + 3) ? ok_le(okey(sqdist_pb(q, b, b + 3)), okey(minSq)) : false;
+    inR = box_valid_i(b + 6, b + 9) ? ok_le(okey(sqdist_pb(q, b + 6, b + 9)), okey(minSq)) : false;
+  }
+  else
+  {
+    inL = box_valid(b, b + 3) ? (sqdist_pb_d(q, b, b + 3) <= minSq) : false;
+    inR = box_valid(b + 6, b + 9) ? (sqdist_pb_d(q, b + 6, b + 9) <= minSq) : false;
+  }
   swap = false;
   if(inL && inR)
   {
     const double cl[3] = {0.5 * (b[0] + b[3]), 0.5 * (b[1] + b[4]), 0.5 * (b[2] + b[5])};
     const double cr[3] = {0.5 * (b[6] + b[9]), 0.5 * (b[7] + b[10]), 0.5 * (b[8] + b[11])};
-    swap = ok_gt(okey(sqdist_pp(q, cl)), okey(sqdist_pp(q, cr)));
+    if constexpr(KEYS)
+      swap = ok_gt(okey(sqdist_pp(q, cl)), okey(sqdist_pp(q, cr)));
+    else
+      swap = sqdist_pp(q, cl) > sqdist_pp(q, cr);
   }
 }
 

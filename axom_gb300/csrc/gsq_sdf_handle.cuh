@@ -5,6 +5,8 @@
 
 #include "gsq_sdf_mixed.cuh"
 
+#include <mutex>
+
 using gsq::NodeRec32;
 using gsq::NodeRec64;
 
@@ -27,6 +29,7 @@ struct gsq_sdf
   float mesh_max = 0.f;          // max |coordinate| of the mesh, rounded up
   unsigned long long* d_audit = nullptr;
   int* d_work = nullptr;          // work-queue counter of the persistent query kernel
+  std::mutex work_busy;           // held by the evaluation using d_work
   gsq::MeshInfo* d_mesh = nullptr; // the single mesh's entry for the query kernel
   long long audit[4] = {0, 0, 0, 0};
   int* d_err = nullptr;

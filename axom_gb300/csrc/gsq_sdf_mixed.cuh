@@ -256,7 +256,7 @@ __device__ __forceinline__ void leaf_refine(const LeafRec<NPC>* __restrict__ lea
   {
     if(!(need & (1 << s))) continue;
     const double* T[3] = {w, w + 3 * (s + 1), w + 3 * (s + 2)};
-    check_triangle<NPC>(q, mc, T, leaves64, leafpos, s, computeNormal);
+    check_triangle<NPC, false>(q, mc, T, leaves64, leafpos, s, computeNormal);
   }
 }
 
@@ -280,13 +280,13 @@ __device__ __forceinline__ bool mixed_traverse(const double* q, MinCand& mc, con
       if(AUDIT)
       {
         bool a2, b2, w2;
-        visit_fp64(nodes64, cur, q, mc.minSq, a2, b2, w2);
+        visit_fp64<false>(nodes64, cur, q, mc.minSq, a2, b2, w2);
         if(a2 != inL || b2 != inR || (inL && inR && w2 != swap)) ++stats[0];
       }
       return;
     }
     if(AUDIT) ++stats[1];
-    visit_fp64(nodes64, cur, q, mc.minSq, inL, inR, swap);
+    visit_fp64<false>(nodes64, cur, q, mc.minSq, inL, inR, swap);
   };
   auto leaf = [&](int leafpos) {
     const int need = leaf_prefilter<NPC>(leaves32, leafpos, c);

@@ -260,7 +260,7 @@ __global__ void __launch_bounds__(128, 5) k_sdf_mixed(const NodeRec64* __restric
       if(p == P_NODE)
       {
         bool inL, inR, swap;
-        visit_fp64(nodes64, cur, q, mc.minSq, inL, inR, swap);
+        visit_fp64<false>(nodes64, cur, q, mc.minSq, inL, inR, swap);
         if(AUDIT) ++st[1];
         apply_visit(inL, inR, swap, pch);
       }
@@ -400,7 +400,7 @@ __global__ void __launch_bounds__(128, 5) k_sdf_mixed(const NodeRec64* __restric
           if(reset) init_min(s1);
           for(int j = 0; j < np; ++j) leaf_refine<NPC>(leaves64, pq[j] >> 2, pq[j] & 3, q, s1, computeNormal);
           bool a2, b2, w2;
-          visit_fp64(nodes64, cur, q, s1.minSq, a2, b2, w2);
+          visit_fp64<false>(nodes64, cur, q, s1.minSq, a2, b2, w2);
           if(a2 != inL || b2 != inR || (inL && inR && w2 != swap)) ++st[0];
         }
         apply_visit(inL, inR, swap, ch);

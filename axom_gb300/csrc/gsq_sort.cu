@@ -337,7 +337,12 @@ int radix_sort_pairs_prealloc(uint32_t* keys[2], int* vals[2], int n, int end_bi
   return cur;
 }
 
-int exclusive_scan(const int* d_in, int* d_out, int m, long long* d_total, cudaStream_t s)
+size_t exclusive_scan_work_bytes(int m)
+{
+  return sizeof(long long) * (size_t)std::max<long long>(1, ((long long)m + SCAN_TILE - 1) / SCAN_TILE);
+}
+
+int exclusive_scan(const int* d_in, int* d_out, int m, long long* d_total, cudaStream_t s, void* work)
 {
   if(m <= 0)
   {
@@ -345,11 +350,16 @@ int exclusive_scan(const int* d_in, int* d_out, int m, long long* d_total, cudaS
     return GSQ_OK;
   }
   const int nb = (int)(((long long)m + SCAN_TILE - 1) / SCAN_TILE);
-  Scratch sums;
-  GSQ_CUDA_TRY(sums.alloc(sizeof(long long) * nb, s));
-  k_scan_tiles<<<nb, SCAN_THREADS, 0, s>>>(d_in, m, sums.as<long long>());
-  k_scan_sums<<<1, SCAN_THREADS, 0, s>>>(sums.as<long long>(), nb, d_total);
-  k_scan_apply<<<nb, SCAN_THREADS, 0, s>>>(d_in, d_out, m, sums.as<long long>());
+  Scratch own;
+  long long* sums = static_cast<long long*>(work);
+  if(!sums)
+  {
+    GSQ_CUDA_TRY(own.alloc(sizeof(long long) * nb, s));
+    sums = own.as<long long>();
+  }
+  k_scan_tiles<<<nb, SCAN_THREADS, 0, s>>>(d_in, m, sums);
+  k_scan_sums<<<1, SCAN_THREADS, 0, s>>>(sums, nb, d_total);
+  k_scan_apply<<<nb, SCAN_THREADS, 0, s>>>(d_in, d_out, m, sums);
   count_launch(3);
   GSQ_CUDA_TRY(cudaGetLastError());
   return GSQ_OK;

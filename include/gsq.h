@@ -28,6 +28,12 @@
  *     layout of primal::Point<double,3>.
  *   - Device work runs on the CUDA device that is current when the handle is
  *     created; a handle must be used with that device current.
+ *   - Like the reference's const BVH::find* and SignedDistance::
+ *     computeDistances, gsq_bvh_find_* and gsq_sdf_eval may run concurrently
+ *     on one handle from several host threads (each on its own stream): a
+ *     call that finds the handle's scratch in use allocates its own.  Builds,
+ *     option changes and destruction must not overlap other calls on the
+ *     handle.
  */
 #ifndef GSQ_H_
 #define GSQ_H_

@@ -114,3 +114,44 @@ def test_full_size_sample(gsq, port):
     h = port.sdf(v[:, 0], v[:, 1], v[:, 2], f)
     pd, _, _ = port.sdf_eval(h, qs, threads=16)
     assert_bits_equal(d[idx], pd, "distance sample")
+
+
+def test_concurrent_calls_on_one_handle(gsq):
+    """computeDistances and the BVH's find* are const and re-entrant in the
+    reference: four host threads, each on its own stream, evaluate (mixed
+    form) and find on one shared handle at the same time; every result equals
+    the single-threaded one bit for bit."""
+    import threading
+    import torch
+    v, f = W.displaced_icosphere(5, 3)
+    q = torch.from_numpy(W.mixed_queries(v, f, 200_000, 4)).cuda()
+    sd = gsq.SignedDistance(v, f, precision=gsq.PRECISION_MIXED)
+    want = sd.compute_distances(q)
+    boxes = W.random_boxes(50_000, 5)
+    qb = torch.from_numpy(W.random_boxes(50_000, 6) * 1.5 - 0.25).cuda()
+    bvh = gsq.BVH(boxes)
+    want_f = [x.cpu().numpy() for x in bvh.find_bounding_boxes(qb)]
+    errors = []
+
+    def work(k):
+        try:
+            st = torch.cuda.Stream()
+            with torch.cuda.stream(st):
+                for _ in range(3):
+                    d = sd.compute_distances(q)
+                    got_f = bvh.find_bounding_boxes(qb)
+                    st.synchronize()
+                    if not torch.equal(d.view(torch.int64), want.view(torch.int64)):
+                        errors.append(f"thread {k}: distances differ")
+                    for x, y in zip(got_f, want_f):
+                        if not np.array_equal(x.cpu().numpy(), y):
+                            errors.append(f"thread {k}: candidates differ")
+        except Exception as e:  # reported below
+            errors.append(f"thread {k}: {e!r}")
+
+    threads = [threading.Thread(target=work, args=(k,)) for k in range(4)]
+    for t in threads:
+        t.start()
+    for t in threads:
+        t.join()
+    assert not errors, errors[:4]
