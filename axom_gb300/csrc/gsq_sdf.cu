@@ -459,15 +459,15 @@ int gsq_sdf_eval(const gsq_sdf* hc, const double* qx, const double* qy, const do
   const bool audit = mixed && h->opts.audit;
   if(audit) GSQ_CUDA_TRY(cudaMemsetAsync(h->d_audit, 0, 4 * sizeof(unsigned long long), s));
   cudaEventRecord(e0, s);
+  // the persistent kernel's work counter: the handle's, held until this call
+  // has synchronised its stream below, or the call's own when another thread
+  // is evaluating on this handle (computeDistances is const and re-entrant)
+  std::unique_lock<std::mutex> work_lock(h->work_busy, std::defer_lock);
+  Scratch own_work;
   if(mixed)
   {
-    // the persistent kernel's work counter: the handle's, or the call's own
-    // when another thread is evaluating on this handle (computeDistances is
-    // const and re-entrant)
-    std::unique_lock<std::mutex> lock(h->work_busy, std::try_to_lock);
-    Scratch own_work;
     int* work = h->d_work;
-    if(!lock.owns_lock())
+    if(!work_lock.try_lock())
     {
       GSQ_CUDA_TRY(own_work.alloc(sizeof(int), s));
       work = own_work.as<int>();
@@ -516,7 +516,8 @@ int gsq_sdf_eval(const gsq_sdf* hc, const double* qx, const double* qy, const do
 // cudaMalloc/cudaFree (this call waits only for its own stream, to read the
 // device error flag).  For them gsq_sdf_eval_noalloc takes the query points
 // and the output in device memory and keeps its only scratch -- the
-// Morton-order sort of the queries -- in the fixed array below, which every
+// Morton-order sort of the queries and the query kernel's work counter -- in
+// the fixed array below, which every
 // GPU that loads this library holds until the process exits.  The array's
 // address is looked up once per device and kept; a cudaDeviceReset, which
 // also invalidates every handle, is not supported after the first call.
@@ -526,7 +527,9 @@ constexpr int NOALLOC_MAX = GSQ_NOALLOC_MAX_QUERIES;
 // keys[2] + vals[2] (4 arrays of NOALLOC_MAX words) + the sort's histogram and
 // look-back words for NOALLOC_MAX keys (4*256 + 64 tiles * 256 + 32 words).
 constexpr size_t NOALLOC_SORT_WORDS = 4 * 256 + ((NOALLOC_MAX + 4095) / 4096) * 256 + 32;
-constexpr size_t NOALLOC_BYTES = sizeof(uint32_t) * (4 * (size_t)NOALLOC_MAX + NOALLOC_SORT_WORDS);
+// ... followed by the persistent kernel's work counter (so that these calls do
+// not share the handle's counter with gsq_sdf_eval).
+constexpr size_t NOALLOC_BYTES = sizeof(uint32_t) * (4 * (size_t)NOALLOC_MAX + NOALLOC_SORT_WORDS + 64);
 static __device__ __align__(256) unsigned char g_noalloc_scratch[NOALLOC_BYTES];
 
 constexpr int NOALLOC_MAX_DEVICES = 64;
@@ -583,6 +586,7 @@ int gsq_sdf_eval_noalloc(const gsq_sdf* hc, const double* qx, const double* qy, 
   int* vals[2] = {reinterpret_cast<int*>(words + 2 * (size_t)NOALLOC_MAX),
                   reinterpret_cast<int*>(words + 3 * (size_t)NOALLOC_MAX)};
   void* sort_work = words + 4 * (size_t)NOALLOC_MAX;
+  int* work = reinterpret_cast<int*>(words + 4 * (size_t)NOALLOC_MAX + NOALLOC_SORT_WORDS);
 
   QueryPts qp {qx, qy, qz, stride};
   const BvhDev* B = bvh_dev(h->bvh);
@@ -610,7 +614,7 @@ int gsq_sdf_eval_noalloc(const gsq_sdf* hc, const double* qx, const double* qy, 
   if(h->opts.precision == GSQ_PRECISION_MIXED)
   {
     rc = mixed_launch(h->npc, B->nodes, h->nodes32, h->leaves, h->leaves32, h->d_mesh, qp, m, order, prm, out,
-                      nullptr, nullptr, h->d_err, nullptr, h->d_work, h->opts.block_size, h->opts.queue_depth, s);
+                      nullptr, nullptr, h->d_err, nullptr, work, h->opts.block_size, h->opts.queue_depth, s);
     if(rc) return rc;
   }
   else

@@ -216,17 +216,19 @@ int gsq_sdf_eval(const gsq_sdf* sdf, const double* qx, const double* qy, const d
  *     (else GSQ_ERR_INVALID).  Returns after its stream has finished (it
  *     reads the device error flag), as gsq_sdf_eval does.
  *   - m <= GSQ_NOALLOC_MAX_QUERIES, else GSQ_ERR_INVALID and nothing runs.
- *   - Calls no cudaMalloc/cudaFree or allocating library routine.  The only
- *     scratch (the Morton-order sort of the points) is one fixed array of
- *     about 4.3 MB in the library's device image, which every GPU that loads
- *     the library holds until the process exits.
+ *   - Calls no cudaMalloc/cudaFree or allocating library routine.  Its only
+ *     scratch (the Morton-order sort of the points and the query kernel's
+ *     work counter) is one fixed array of about 4.3 MB in the library's
+ *     device image, which every GPU that loads the library holds until the
+ *     process exits.
  *   - The first call on each device looks the array's device address up once
  *     (cudaGetSymbolAddress) and keeps it; make that first call before any
  *     stream capture.  A cudaDeviceReset after it is not supported (it also
  *     invalidates every handle).
- *   - Every call shares that one array: calls whose GPU work overlaps (other
- *     streams or host threads, on the same device) race and corrupt each
- *     other's results.  Serialise them.
+ *   - Every call shares that one array: calls of this entry point whose GPU
+ *     work overlaps (other streams or host threads, on the same device) race
+ *     and corrupt each other's results.  Serialise them.  (A gsq_sdf_eval
+ *     running at the same time does not use the array.)
  *   - The precision and query-order options of the handle apply; outputs equal
  *     gsq_sdf_eval's. */
 #define GSQ_NOALLOC_MAX_QUERIES 262144
