@@ -208,12 +208,12 @@ __device__ __forceinline__ uint32_t box_morton(const double* __restrict__ box, c
   return spread10(q[0]) | (spread10(q[1]) << 1) | (spread10(q[2]) << 2);
 }
 
-// delta (BR:265-287)
-__device__ __forceinline__ int delta(int a, int b, int inner, const uint32_t* __restrict__ codes)
+// delta (BR:265-287); ca is codes[a], loaded once by the caller
+__device__ __forceinline__ int delta(int a, uint32_t ca, int b, int inner, const uint32_t* __restrict__ codes)
 {
   const bool oor = (b < 0 || b > inner);
   const int bb = oor ? 0 : b;
-  uint32_t x = __ldg(codes + a) ^ __ldg(codes + bb);
+  uint32_t x = ca ^ __ldg(codes + bb);
   const bool tie = (x == 0);
   if(tie) x = (uint32_t)a ^ (uint32_t)bb;
   int c = __clz(x);
@@ -229,20 +229,26 @@ __device__ __forceinline__ void karras_node(int i, const uint32_t* __restrict__ 
                                             NodeRec64* __restrict__ nodes)
 {
   const int inner = n - 1;
-  const int dir = (delta(i, i + 1, inner, codes) - delta(i, i - 1, inner, codes)) < 0 ? -1 : 1;
-  const int dmin = delta(i, i - dir, inner, codes);
+  const uint32_t ci = __ldg(codes + i);
+  const int dir = (delta(i, ci, i + 1, inner, codes) - delta(i, ci, i - 1, inner, codes)) < 0 ? -1 : 1;
+  const int dmin = delta(i, ci, i - dir, inner, codes);
   int lmax = 2;
-  while(delta(i, i + lmax * dir, inner, codes) > dmin) lmax *= 2;
+  while(delta(i, ci, i + lmax * dir, inner, codes) > dmin) lmax *= 2;
   int l = 0;
   for(int s = lmax / 2; s >= 1; s /= 2)
-    if(delta(i, i + (l + s) * dir, inner, codes) > dmin) l += s;
+    if(delta(i, ci, i + (l + s) * dir, inner, codes) > dmin) l += s;
   const int j = i + l * dir;
-  const int dnode = delta(i, j, inner, codes);
+  const int dnode = delta(i, ci, j, inner, codes);
   int s = 0;
-  double div = 2.0;
-  for(int st = (int)ceil(double(float(l)) / div);; div *= 2.0, st = (int)ceil(double(float(l)) / div))
+  // The reference's step is ceil(float32(l) / div) in FloatType = double with
+  // div = 2, 4, 8, ...: float32(l) is an integer L and dividing it by a power
+  // of two is exact, so the step is ceil(L / 2^k) = (L + 2^k - 1) >> k,
+  // computed here without FP64 arithmetic (scarce on this GPU).
+  const long long L = (long long)(float)l;
+  for(int k = 1;; ++k)
   {
-    if(delta(i, i + (s + st) * dir, inner, codes) > dnode) s += st;
+    const int st = (int)((L + (1LL << k) - 1) >> k);
+    if(delta(i, ci, i + (s + st) * dir, inner, codes) > dnode) s += st;
     if(st == 1) break;
   }
   const int split = i + s * dir + min(dir, 0);
@@ -328,6 +334,48 @@ __device__ __forceinline__ int atomic_add_acq_rel(int* p, int v)
   return old;
 }
 
+// One level of the refit: node `last` (leaf id inner + k, or an inner node)
+// with box (lo, hi) publishes the box into its parent `node`'s record and
+// bumps the parent's counter.  Returns true when this thread continues: it
+// arrived second, (lo, hi) is now the parent's box, last the parent and node
+// the grandparent.  At the root the box goes to root_box and it returns false.
+__device__ __forceinline__ bool refit_step(int& last, int& node, double* lo, double* hi,
+                                           const int* __restrict__ lchild, const int* __restrict__ parent,
+                                           int* __restrict__ counters, NodeRec64* nodes, double* __restrict__ root_box)
+{
+  const int side = (lchild[node] == last) ? 0 : 1;
+  double* dst = nodes[node].b + 6 * side;
+  for(int d = 0; d < 3; ++d)
+  {
+    dst[d] = lo[d];
+    dst[3 + d] = hi[d];
+  }
+  if(atomic_add_acq_rel(&counters[node], 1) == 0) return false;
+  const double* b = nodes[node].b;
+  double llo[3], lhi[3];
+  for(int d = 0; d < 3; ++d)
+  {
+    lo[d] = __ldcg(b + 6 + d);  // right child box
+    hi[d] = __ldcg(b + 9 + d);
+    llo[d] = __ldcg(b + d);     // left child box
+    lhi[d] = __ldcg(b + 3 + d);
+  }
+  add_box(lo, hi, llo, lhi);
+  last = node;
+  node = parent[node];
+  if(node == -1)
+  {
+    if(root_box)
+      for(int d = 0; d < 3; ++d)
+      {
+        root_box[d] = lo[d];
+        root_box[3 + d] = hi[d];
+      }
+    return false;
+  }
+  return true;
+}
+
 // propagate_aabbs (BR:505-576) fused with emit_bvh_parents (LB:225-264), for
 // sorted leaf k with box (lo, hi) of a hierarchy over n leaves.  The thread
 // stores its box into its parent's record and bumps the parent's counter with
@@ -339,41 +387,10 @@ __device__ __forceinline__ void refit_leaf(int k, double* lo, double* hi, int n,
                                            const int* __restrict__ parent, int* __restrict__ counters,
                                            NodeRec64* nodes, double* __restrict__ root_box)
 {
-  const int inner = n - 1;
-  int last = inner + k;
-  int node = parent[inner + k];
-  while(true)
+  int last = n - 1 + k;
+  int node = parent[last];
+  while(refit_step(last, node, lo, hi, lchild, parent, counters, nodes, root_box))
   {
-    const int side = (lchild[node] == last) ? 0 : 1;
-    double* dst = nodes[node].b + 6 * side;
-    for(int d = 0; d < 3; ++d)
-    {
-      dst[d] = lo[d];
-      dst[3 + d] = hi[d];
-    }
-    if(atomic_add_acq_rel(&counters[node], 1) == 0) return;
-    const double* b = nodes[node].b;
-    double llo[3], lhi[3];
-    for(int d = 0; d < 3; ++d)
-    {
-      lo[d] = __ldcg(b + 6 + d);  // right child box
-      hi[d] = __ldcg(b + 9 + d);
-      llo[d] = __ldcg(b + d);     // left child box
-      lhi[d] = __ldcg(b + 3 + d);
-    }
-    add_box(lo, hi, llo, lhi);
-    last = node;
-    node = parent[node];
-    if(node == -1)
-    {
-      if(root_box)
-        for(int d = 0; d < 3; ++d)
-        {
-          root_box[d] = lo[d];
-          root_box[3 + d] = hi[d];
-        }
-      return;
-    }
   }
 }
 }  // namespace lbvh

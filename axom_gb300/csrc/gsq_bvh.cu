@@ -11,10 +11,11 @@
 //   radix sort      stable (key, index) sort (sort_mcodes, BR:225-260)
 //   k_karras        Karras 2012 hierarchy, identical tie-breaking (build_tree,
 //                   BR:265-384)
-//   k_refit         bottom-up boxes with one atomic per node; the second
+//   k_refit_persist bottom-up boxes with one atomic per node; the second
 //                   arrival continues (propagate_aabbs, BR:505-576), writing each
 //                   box straight into its parent's 128-byte node record (the
-//                   emit step fused in).  No thread ever waits on another.
+//                   emit step fused in); persistent lanes take the next leaf
+//                   when their chain ends.  No thread ever waits on another.
 // Queries (replace findCandidatesImpl, LinearBVH.hpp:271-402): one thread per
 // query runs the reference traversal state machine (bvh_traverse.hpp:66-154);
 // pass 1 keeps up to CAP candidates per query in scratch and counts all of
@@ -111,26 +112,60 @@ __global__ void __launch_bounds__(BUILD_THREADS) k_karras(const uint32_t* __rest
   lbvh::karras_node(i, codes, n, lchild, rchild, parent, nodes);
 }
 
-// One thread per sorted leaf (lbvh::refit_leaf).
-__global__ void __launch_bounds__(BUILD_THREADS) k_refit(const double* __restrict__ leaf,
-                                                           const int* __restrict__ perm,
-                                                           int n,
-                                                           const int* __restrict__ lchild,
-                                                           const int* __restrict__ parent,
-                                                           int* __restrict__ counters,
-                                                           NodeRec64* nodes,
-                                                           double* __restrict__ root_box)
+// The refit as a persistent loop: every lane takes the next sorted leaf from
+// a work counter (one warp-aggregated atomic) when its previous chain has
+// ended, then climbs one level per iteration (lbvh::refit_step).  One thread
+// per leaf leaves warps on a few lanes after the first levels (half the
+// threads stop at each level); here the lanes stay busy.  Nothing waits: a
+// lane's chain ends at its first first-arrival or at the root.
+__global__ void __launch_bounds__(BUILD_THREADS) k_refit_persist(const double* __restrict__ leaf,
+                                                                   const int* __restrict__ perm,
+                                                                   int n,
+                                                                   const int* __restrict__ lchild,
+                                                                   const int* __restrict__ parent,
+                                                                   int* __restrict__ counters,
+                                                                   NodeRec64* nodes,
+                                                                   double* __restrict__ root_box,
+                                                                   int* __restrict__ work)
 {
-  const int k = blockIdx.x * blockDim.x + threadIdx.x;
-  if(k >= n) return;
-  const int id = perm[k];
-  double lo[3], hi[3];
-  for(int d = 0; d < 3; ++d)
+  constexpr unsigned FULL = 0xFFFFFFFFu;
+  const int lane = threadIdx.x & 31;
+  const unsigned lt_mask = (1u << lane) - 1u;
+  const int inner = n - 1;
+  bool active = false, open = true;
+  int last = 0, node = 0;
+  double lo[3] = {0.0, 0.0, 0.0}, hi[3] = {0.0, 0.0, 0.0};
+  while(true)
   {
-    lo[d] = leaf[6 * (size_t)id + d];
-    hi[d] = leaf[6 * (size_t)id + 3 + d];
+    const unsigned want = __ballot_sync(FULL, !active && open);
+    if(want)
+    {
+      const int leader = __ffs(want) - 1;
+      int base = 0;
+      if(lane == leader) base = atomicAdd(work, __popc(want));
+      base = __shfl_sync(FULL, base, leader);
+      if(!active && open)
+      {
+        const int k = base + __popc(want & lt_mask);
+        if(k < n)
+        {
+          const int id = perm[k];
+          for(int d = 0; d < 3; ++d)
+          {
+            lo[d] = leaf[6 * (size_t)id + d];
+            hi[d] = leaf[6 * (size_t)id + 3 + d];
+          }
+          last = inner + k;
+          node = parent[inner + k];
+          active = true;
+        }
+        else
+          open = false;
+      }
+    }
+    if(__ballot_sync(FULL, active || open) == 0) break;
+    if(active) active = lbvh::refit_step(last, node, lo, hi, lchild, parent, counters, nodes, root_box);
   }
-  lbvh::refit_leaf(k, lo, hi, n, lchild, parent, counters, nodes, root_box);
 }
 
 // ---- traversal --------------------------------------------------------------
@@ -472,7 +507,7 @@ size_t build_scratch_layout(int n, char* base, BuildScratch* out)
   const size_t sz_params = align256(sizeof(double) * 18);
   const size_t sz_u32 = align256(sizeof(uint32_t) * n);
   const size_t sz_par = align256(sizeof(int) * (2 * (size_t)n - 1));
-  const size_t sz_cnt = align256(sizeof(int) * inner);
+  const size_t sz_cnt = align256(sizeof(int) * (inner + 1));  // node counters, then the refit's work counter
   const size_t sz_fold = align256(sizeof(Fold) * fold_blocks);
   const size_t sz_sort = align256(radix_sort_work_bytes(n));
   const size_t total = sz_leaf + sz_params + 4 * sz_u32 + sz_par + sz_cnt + sz_fold + sz_sort;
@@ -520,9 +555,14 @@ int enqueue_build(BvhDev& B, const BuildScratch& w, const double* d_boxes, int n
   GSQ_CUDA_TRY(cudaMemcpyAsync(B.codes, keys[which], sizeof(uint32_t) * n, cudaMemcpyDeviceToDevice, s));
   GSQ_CUDA_TRY(cudaMemcpyAsync(B.perm, vals[which], sizeof(int) * n, cudaMemcpyDeviceToDevice, s));
   k_karras<<<grid_for(inner, BUILD_THREADS), BUILD_THREADS, 0, s>>>(B.codes, n, B.lchild, B.rchild, w.parent, B.nodes);
-  GSQ_CUDA_TRY(cudaMemsetAsync(w.counters, 0, sizeof(int) * inner, s));
-  k_refit<<<grid_for(n, BUILD_THREADS), BUILD_THREADS, 0, s>>>(w.leaf, B.perm, n, B.lchild, w.parent, w.counters,
-                                                               B.nodes, w.params + 12);
+  GSQ_CUDA_TRY(cudaMemsetAsync(w.counters, 0, sizeof(int) * (inner + 1), s));
+  int dev = 0, sms = 0, per_sm = 0;
+  GSQ_CUDA_TRY(cudaGetDevice(&dev));
+  GSQ_CUDA_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+  GSQ_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_refit_persist, BUILD_THREADS, 0));
+  const int rgrid = std::max(1, std::min(sms * std::max(per_sm, 1), grid_for(n, BUILD_THREADS)));
+  k_refit_persist<<<rgrid, BUILD_THREADS, 0, s>>>(w.leaf, B.perm, n, B.lchild, w.parent, w.counters, B.nodes,
+                                                  w.params + 12, w.counters + inner);
   count_launch(2);
   GSQ_CUDA_TRY(cudaGetLastError());
   return GSQ_OK;
