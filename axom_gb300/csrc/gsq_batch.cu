@@ -9,7 +9,7 @@
 //   k_b_morton       Morton code of each cell in its mesh's bounds
 //   two stable radix sorts: by code, then by mesh; within a mesh the order is
 //                    (code, cell index), the single-tree sort's order
-//   k_b_karras / k_b_refit / k_b_leaf_records: the single-tree kernels' bodies
+//   k_b_karras / k_b_refit_persist / k_b_leaf_records: the single-tree kernels' bodies
 //                    on each mesh's slice with local indices
 //   mixed_prepare    FP32 node and leaf records
 // Query: each point's Morton code in its mesh's bounds, prefixed by the mesh
@@ -177,26 +177,66 @@ __global__ void __launch_bounds__(BT) k_b_karras(const uint32_t* __restrict__ sc
   lbvh::karras_node((int)(g - io), scodes + c0, n, lchild + io, rchild + io, parent + po, nodes + io);
 }
 
-__global__ void __launch_bounds__(BT) k_b_refit(const double* __restrict__ leafbox, const int* __restrict__ perm,
-                                                const long long* __restrict__ coff, int nm, int ncells,
-                                                const int* __restrict__ lchild, const int* __restrict__ parent,
-                                                int* __restrict__ counters, NodeRec64* nodes, double* __restrict__ params)
+// The segmented refit as a persistent loop (as the single-tree build's
+// k_refit_persist): a lane takes the next cell of any mesh when its previous
+// chain has ended and climbs that mesh's tree one level per iteration.
+__global__ void __launch_bounds__(BT) k_b_refit_persist(const double* __restrict__ leafbox, const int* __restrict__ perm,
+                                                        const long long* __restrict__ coff, int nm, int ncells,
+                                                        const int* __restrict__ lchild, const int* __restrict__ parent,
+                                                        int* __restrict__ counters, NodeRec64* nodes,
+                                                        double* __restrict__ params, int* __restrict__ work)
 {
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if(i >= ncells) return;
-  const int k = segment_of(coff, nm, i);
-  const long long c0 = coff[k];
-  const int n = (int)(coff[k + 1] - c0);
-  const long long io = c0 - k, po = 2 * c0 - k;
-  const int id = perm[i];
-  double lo[3], hi[3];
-  for(int d = 0; d < 3; ++d)
+  constexpr unsigned FULL = 0xFFFFFFFFu;
+  const int lane = threadIdx.x & 31;
+  const unsigned lt_mask = (1u << lane) - 1u;
+  bool active = false, open = true;
+  int last = 0, node = 0;
+  double lo[3] = {0.0, 0.0, 0.0}, hi[3] = {0.0, 0.0, 0.0};
+  const int* lc = lchild;
+  const int* pa = parent;
+  int* cn = counters;
+  NodeRec64* nd = nodes;
+  double* root = params;
+  while(true)
   {
-    lo[d] = leafbox[6 * (size_t)id + d];
-    hi[d] = leafbox[6 * (size_t)id + 3 + d];
+    const unsigned want = __ballot_sync(FULL, !active && open);
+    if(want)
+    {
+      const int leader = __ffs(want) - 1;
+      int base = 0;
+      if(lane == leader) base = atomicAdd(work, __popc(want));
+      base = __shfl_sync(FULL, base, leader);
+      if(!active && open)
+      {
+        const int i = base + __popc(want & lt_mask);
+        if(i < ncells)
+        {
+          const int k = segment_of(coff, nm, i);
+          const long long c0 = coff[k];
+          const int n = (int)(coff[k + 1] - c0);
+          const long long io = c0 - k, po = 2 * c0 - k;
+          lc = lchild + io;
+          pa = parent + po;
+          cn = counters + io;
+          nd = nodes + io;
+          root = params + (size_t)PARAMS * k + 12;
+          const int id = perm[i];
+          for(int d = 0; d < 3; ++d)
+          {
+            lo[d] = leafbox[6 * (size_t)id + d];
+            hi[d] = leafbox[6 * (size_t)id + 3 + d];
+          }
+          last = (n - 1) + (int)(i - c0);
+          node = pa[last];
+          active = true;
+        }
+        else
+          open = false;
+      }
+    }
+    if(__ballot_sync(FULL, active || open) == 0) break;
+    if(active) active = lbvh::refit_step(last, node, lo, hi, lc, pa, cn, nd, root);
   }
-  lbvh::refit_leaf((int)(i - c0), lo, hi, n, lchild + io, parent + po, counters + io, nodes + io,
-                   params + (size_t)PARAMS * k + 12);
 }
 
 template <int NPC>
@@ -403,9 +443,14 @@ int enqueue_build(gsq_batch* h, cudaStream_t s)
   k_b_gather<<<grid_for(C, BT), BT, 0, s>>>(v2[w2], h->codes, C, h->perm, h->scodes);
   k_b_karras<<<grid_for(h->ninner, BT), BT, 0, s>>>(h->scodes, h->coff, nm, (int)h->ninner, h->lchild, h->rchild,
                                                     h->parent, h->nodes);
-  GSQ_CUDA_TRY(cudaMemsetAsync(h->counters, 0, sizeof(int) * h->ninner, s));
-  k_b_refit<<<grid_for(C, BT), BT, 0, s>>>(h->leafbox, h->perm, h->coff, nm, C, h->lchild, h->parent, h->counters,
-                                           h->nodes, h->params);
+  GSQ_CUDA_TRY(cudaMemsetAsync(h->counters, 0, sizeof(int) * (h->ninner + 1), s));
+  int dev = 0, sms = 0, per_sm = 0;
+  GSQ_CUDA_TRY(cudaGetDevice(&dev));
+  GSQ_CUDA_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+  GSQ_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_b_refit_persist, BT, 0));
+  const int rgrid = std::max(1, std::min(sms * std::max(per_sm, 1), grid_for(C, BT)));
+  k_b_refit_persist<<<rgrid, BT, 0, s>>>(h->leafbox, h->perm, h->coff, nm, C, h->lchild, h->parent, h->counters,
+                                         h->nodes, h->params, h->counters + h->ninner);
   if(h->npc == 3)
     k_b_leaf_records<3><<<grid_for(C, BT), BT, 0, s>>>(h->perm, h->coff, h->voff, nm, C, h->x, h->y, h->z, h->cells,
                                                        static_cast<LeafRec<3>*>(h->leaves));
@@ -614,7 +659,7 @@ int gsq_batch_create(gsq_batch** out, int32_t nmeshes, const int64_t* vert_offse
       {(void**)&h->parent, sizeof(int) * (2 * Cn - nmeshes)},
       {(void**)&h->lchild, sizeof(int) * h->ninner},
       {(void**)&h->rchild, sizeof(int) * h->ninner},
-      {(void**)&h->counters, sizeof(int) * h->ninner},
+      {(void**)&h->counters, sizeof(int) * (h->ninner + 1)},  // node counters, then the refit's work counter
       {(void**)&h->nodes, sizeof(NodeRec64) * h->ninner},
       {(void**)&h->nodes32, sizeof(NodeRec32) * h->ninner},
       {(void**)&h->leaves, leaf_bytes * Cn},

@@ -334,6 +334,13 @@ __device__ __forceinline__ int atomic_add_acq_rel(int* p, int v)
   return old;
 }
 
+// propagate_aabbs (BR:505-576) fused with emit_bvh_parents (LB:225-264), one
+// level at a time: a thread stores its node's box into the parent's record and
+// bumps the parent's counter with an acquire-release atomic (the store is
+// visible to the second arrival, which sees the first arrival's box); the first
+// arrival stops and the second combines the two child boxes as the reference's
+// SEQ order does (box(node) = addBox(box(right), box(left))) and moves up.  No
+// thread ever waits on another.
 // One level of the refit: node `last` (leaf id inner + k, or an inner node)
 // with box (lo, hi) publishes the box into its parent `node`'s record and
 // bumps the parent's counter.  Returns true when this thread continues: it
@@ -376,22 +383,5 @@ __device__ __forceinline__ bool refit_step(int& last, int& node, double* lo, dou
   return true;
 }
 
-// propagate_aabbs (BR:505-576) fused with emit_bvh_parents (LB:225-264), for
-// sorted leaf k with box (lo, hi) of a hierarchy over n leaves.  The thread
-// stores its box into its parent's record and bumps the parent's counter with
-// an acquire-release atomic (the store is visible to the second arrival, which
-// sees the first arrival's box); the first arrival exits and the second combines the two child
-// boxes as the reference's SEQ order does (box(node) = addBox(box(right),
-// box(left))) and moves up.  No thread ever waits on another.
-__device__ __forceinline__ void refit_leaf(int k, double* lo, double* hi, int n, const int* __restrict__ lchild,
-                                           const int* __restrict__ parent, int* __restrict__ counters,
-                                           NodeRec64* nodes, double* __restrict__ root_box)
-{
-  int last = n - 1 + k;
-  int node = parent[last];
-  while(refit_step(last, node, lo, hi, lchild, parent, counters, nodes, root_box))
-  {
-  }
-}
 }  // namespace lbvh
 }  // namespace gsq
