@@ -182,17 +182,16 @@ __global__ void __launch_bounds__(BT) k_b_karras(const uint32_t* __restrict__ sc
 // chain has ended and climbs that mesh's tree one level per iteration.
 __global__ void __launch_bounds__(BT) k_b_refit_persist(const double* __restrict__ leafbox, const int* __restrict__ perm,
                                                         const long long* __restrict__ coff, int nm, int ncells,
-                                                        const int* __restrict__ lchild, const int* __restrict__ parent,
-                                                        int* __restrict__ counters, NodeRec64* nodes,
-                                                        double* __restrict__ params, int* __restrict__ work)
+                                                        const int* __restrict__ parent, int* __restrict__ counters,
+                                                        NodeRec64* nodes, double* __restrict__ params,
+                                                        int* __restrict__ work)
 {
   constexpr unsigned FULL = 0xFFFFFFFFu;
   const int lane = threadIdx.x & 31;
   const unsigned lt_mask = (1u << lane) - 1u;
   bool active = false, open = true;
-  int last = 0, node = 0;
+  int pcode = 0;
   double lo[3] = {0.0, 0.0, 0.0}, hi[3] = {0.0, 0.0, 0.0};
-  const int* lc = lchild;
   const int* pa = parent;
   int* cn = counters;
   NodeRec64* nd = nodes;
@@ -215,7 +214,6 @@ __global__ void __launch_bounds__(BT) k_b_refit_persist(const double* __restrict
           const long long c0 = coff[k];
           const int n = (int)(coff[k + 1] - c0);
           const long long io = c0 - k, po = 2 * c0 - k;
-          lc = lchild + io;
           pa = parent + po;
           cn = counters + io;
           nd = nodes + io;
@@ -226,8 +224,7 @@ __global__ void __launch_bounds__(BT) k_b_refit_persist(const double* __restrict
             lo[d] = leafbox[6 * (size_t)id + d];
             hi[d] = leafbox[6 * (size_t)id + 3 + d];
           }
-          last = (n - 1) + (int)(i - c0);
-          node = pa[last];
+          pcode = pa[(n - 1) + (int)(i - c0)];
           active = true;
         }
         else
@@ -235,7 +232,7 @@ __global__ void __launch_bounds__(BT) k_b_refit_persist(const double* __restrict
       }
     }
     if(__ballot_sync(FULL, active || open) == 0) break;
-    if(active) active = lbvh::refit_step(last, node, lo, hi, lc, pa, cn, nd, root);
+    if(active) active = lbvh::refit_step(pcode, lo, hi, pa, cn, nd, root);
   }
 }
 
@@ -280,7 +277,7 @@ __global__ void __launch_bounds__(BT) k_b_depth(const long long* __restrict__ co
   {
     const int p = par[node];
     if(p < 0) break;
-    node = p;
+    node = p >> 1;
     ++d;
   }
   atomicMax(max_depth, d);
@@ -449,8 +446,8 @@ int enqueue_build(gsq_batch* h, cudaStream_t s)
   GSQ_CUDA_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
   GSQ_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_b_refit_persist, BT, 0));
   const int rgrid = std::max(1, std::min(sms * std::max(per_sm, 1), grid_for(C, BT)));
-  k_b_refit_persist<<<rgrid, BT, 0, s>>>(h->leafbox, h->perm, h->coff, nm, C, h->lchild, h->parent, h->counters,
-                                         h->nodes, h->params, h->counters + h->ninner);
+  k_b_refit_persist<<<rgrid, BT, 0, s>>>(h->leafbox, h->perm, h->coff, nm, C, h->parent, h->counters, h->nodes,
+                                         h->params, h->counters + h->ninner);
   if(h->npc == 3)
     k_b_leaf_records<3><<<grid_for(C, BT), BT, 0, s>>>(h->perm, h->coff, h->voff, nm, C, h->x, h->y, h->z, h->cells,
                                                        static_cast<LeafRec<3>*>(h->leaves));

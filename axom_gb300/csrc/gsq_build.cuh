@@ -223,7 +223,8 @@ __device__ __forceinline__ int delta(int a, uint32_t ca, int b, int inner, const
 
 // build_tree (BR:290-384) for inner node i of a hierarchy over n sorted codes;
 // also writes the child links of the node record.  Leaf j has node id
-// inner + j in lchild/rchild/parent.
+// inner + j in lchild/rchild/parent; parent[x] holds the parent's id times two
+// plus the side of x (0 left, 1 right), -1 at the root.
 __device__ __forceinline__ void karras_node(int i, const uint32_t* __restrict__ codes, int n, int* __restrict__ lchild,
                                             int* __restrict__ rchild, int* __restrict__ parent,
                                             NodeRec64* __restrict__ nodes)
@@ -255,22 +256,22 @@ __device__ __forceinline__ void karras_node(int i, const uint32_t* __restrict__ 
   int lc, rc;
   if(min(i, j) == split)
   {
-    parent[split + inner] = i;
+    parent[split + inner] = 2 * i;
     lc = split + inner;
   }
   else
   {
-    parent[split] = i;
+    parent[split] = 2 * i;
     lc = split;
   }
   if(max(i, j) == split + 1)
   {
-    parent[split + inner + 1] = i;
+    parent[split + inner + 1] = 2 * i + 1;
     rc = split + inner + 1;
   }
   else
   {
-    parent[split + 1] = i;
+    parent[split + 1] = 2 * i + 1;
     rc = split + 1;
   }
   lchild[i] = lc;
@@ -341,36 +342,44 @@ __device__ __forceinline__ int atomic_add_acq_rel(int* p, int v)
 // arrival stops and the second combines the two child boxes as the reference's
 // SEQ order does (box(node) = addBox(box(right), box(left))) and moves up.  No
 // thread ever waits on another.
-// One level of the refit: node `last` (leaf id inner + k, or an inner node)
-// with box (lo, hi) publishes the box into its parent `node`'s record and
-// bumps the parent's counter.  Returns true when this thread continues: it
-// arrived second, (lo, hi) is now the parent's box, last the parent and node
-// the grandparent.  At the root the box goes to root_box and it returns false.
-__device__ __forceinline__ bool refit_step(int& last, int& node, double* lo, double* hi,
-                                           const int* __restrict__ lchild, const int* __restrict__ parent,
+// One level of the refit for the node with box (lo, hi) and parent code pcode
+// (parent id * 2 + side).  The parent's own code is read before the atomic,
+// so that its latency overlaps the atomic's; the second arrival reads only
+// its sibling's box back.  Returns true when this thread continues: (lo, hi)
+// is then the parent's box and pcode the parent's code.  At the root the box
+// goes to root_box and it returns false.
+__device__ __forceinline__ bool refit_step(int& pcode, double* lo, double* hi, const int* __restrict__ parent,
                                            int* __restrict__ counters, NodeRec64* nodes, double* __restrict__ root_box)
 {
-  const int side = (lchild[node] == last) ? 0 : 1;
-  double* dst = nodes[node].b + 6 * side;
+  const int node = pcode >> 1, side = pcode & 1;
+  const int next = __ldg(parent + node);
+  double* b = nodes[node].b;
   for(int d = 0; d < 3; ++d)
   {
-    dst[d] = lo[d];
-    dst[3 + d] = hi[d];
+    b[6 * side + d] = lo[d];
+    b[6 * side + 3 + d] = hi[d];
   }
   if(atomic_add_acq_rel(&counters[node], 1) == 0) return false;
-  const double* b = nodes[node].b;
-  double llo[3], lhi[3];
+  double slo[3], shi[3];
   for(int d = 0; d < 3; ++d)
   {
-    lo[d] = __ldcg(b + 6 + d);  // right child box
-    hi[d] = __ldcg(b + 9 + d);
-    llo[d] = __ldcg(b + d);     // left child box
-    lhi[d] = __ldcg(b + 3 + d);
+    slo[d] = __ldcg(b + 6 * (1 - side) + d);
+    shi[d] = __ldcg(b + 6 * (1 - side) + 3 + d);
   }
-  add_box(lo, hi, llo, lhi);
-  last = node;
-  node = parent[node];
-  if(node == -1)
+  if(side == 0)
+  {
+    // this thread holds the left box: start from the right (sibling's) box
+    add_box(slo, shi, lo, hi);
+    for(int d = 0; d < 3; ++d)
+    {
+      lo[d] = slo[d];
+      hi[d] = shi[d];
+    }
+  }
+  else
+    add_box(lo, hi, slo, shi);
+  pcode = next;
+  if(next < 0)
   {
     if(root_box)
       for(int d = 0; d < 3; ++d)

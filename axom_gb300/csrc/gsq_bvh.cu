@@ -121,7 +121,6 @@ __global__ void __launch_bounds__(BUILD_THREADS) k_karras(const uint32_t* __rest
 __global__ void __launch_bounds__(BUILD_THREADS) k_refit_persist(const double* __restrict__ leaf,
                                                                    const int* __restrict__ perm,
                                                                    int n,
-                                                                   const int* __restrict__ lchild,
                                                                    const int* __restrict__ parent,
                                                                    int* __restrict__ counters,
                                                                    NodeRec64* nodes,
@@ -133,7 +132,7 @@ __global__ void __launch_bounds__(BUILD_THREADS) k_refit_persist(const double* _
   const unsigned lt_mask = (1u << lane) - 1u;
   const int inner = n - 1;
   bool active = false, open = true;
-  int last = 0, node = 0;
+  int pcode = 0;
   double lo[3] = {0.0, 0.0, 0.0}, hi[3] = {0.0, 0.0, 0.0};
   while(true)
   {
@@ -155,8 +154,7 @@ __global__ void __launch_bounds__(BUILD_THREADS) k_refit_persist(const double* _
             lo[d] = leaf[6 * (size_t)id + d];
             hi[d] = leaf[6 * (size_t)id + 3 + d];
           }
-          last = inner + k;
-          node = parent[inner + k];
+          pcode = parent[inner + k];
           active = true;
         }
         else
@@ -164,7 +162,7 @@ __global__ void __launch_bounds__(BUILD_THREADS) k_refit_persist(const double* _
       }
     }
     if(__ballot_sync(FULL, active || open) == 0) break;
-    if(active) active = lbvh::refit_step(last, node, lo, hi, lchild, parent, counters, nodes, root_box);
+    if(active) active = lbvh::refit_step(pcode, lo, hi, parent, counters, nodes, root_box);
   }
 }
 
@@ -561,8 +559,8 @@ int enqueue_build(BvhDev& B, const BuildScratch& w, const double* d_boxes, int n
   GSQ_CUDA_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
   GSQ_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_refit_persist, BUILD_THREADS, 0));
   const int rgrid = std::max(1, std::min(sms * std::max(per_sm, 1), grid_for(n, BUILD_THREADS)));
-  k_refit_persist<<<rgrid, BUILD_THREADS, 0, s>>>(w.leaf, B.perm, n, B.lchild, w.parent, w.counters, B.nodes,
-                                                  w.params + 12, w.counters + inner);
+  k_refit_persist<<<rgrid, BUILD_THREADS, 0, s>>>(w.leaf, B.perm, n, w.parent, w.counters, B.nodes, w.params + 12,
+                                                  w.counters + inner);
   count_launch(2);
   GSQ_CUDA_TRY(cudaGetLastError());
   return GSQ_OK;

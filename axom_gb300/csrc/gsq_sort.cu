@@ -10,10 +10,11 @@
 // an atomic tile counter, ranks its keys per digit with warp-aggregated
 // counting (__match_any_sync: one shared-memory update per distinct digit per
 // warp row), and obtains its global offsets by a decoupled look-back over the
-// tiles before it.  Ranks follow input position (warp, row, lane order), so
-// the sort is stable, which makes the result identical to a stable sort of the
-// reference.  Every look-back wait is bounded: after SPIN_LIMIT polls the
-// block sets DEVERR_WAIT and continues.
+// tiles before it (eight predecessors read at once).  Ranks follow input
+// position (warp, row, lane order), so the sort is stable, which makes the
+// result identical to a stable sort of the reference.  Every look-back wait is
+// bounded: after SPIN_LIMIT polls without progress the block sets
+// DEVERR_WAIT and continues.
 #include "gsq_internal.cuh"
 
 #include <algorithm>
@@ -30,7 +31,8 @@ constexpr int RADIX = 256;
 constexpr unsigned FLAG_AGG = 1u << 30; // tile aggregate published
 constexpr unsigned FLAG_PRE = 2u << 30; // inclusive prefix published
 constexpr unsigned VAL_MASK = (1u << 30) - 1;
-constexpr long long SPIN_LIMIT = 1ll << 20;  // polls before a look-back wait gives up
+constexpr long long SPIN_LIMIT = 1ll << 20;  // polls without progress before a look-back wait gives up
+constexpr int LOOK = 8;                  // look-back window (tiles read at once)
 
 __device__ __forceinline__ unsigned ld_volatile(const unsigned* p)
 {
@@ -140,23 +142,33 @@ __global__ void __launch_bounds__(THREADS) k_onesweep(const uint32_t* __restrict
   else
   {
     st_volatile(lb, FLAG_AGG | total);
+    // LOOK tiles are read at once (independent loads), then consumed in order
+    // up to the first unpublished one or the first inclusive prefix
     long long spins = 0;
     for(int k = tile - 1; k >= 0;)
     {
-      const unsigned v = ld_volatile(lookback + (size_t)k * RADIX + d);
-      const unsigned flag = v & ~VAL_MASK;
-      if(flag == 0u)
+      unsigned v[LOOK];
+#pragma unroll
+      for(int u = 0; u < LOOK; ++u) v[u] = (k - u >= 0) ? ld_volatile(lookback + (size_t)(k - u) * RADIX + d) : 0u;
+      int used = 0;
+      bool done = false;
+#pragma unroll
+      for(int u = 0; u < LOOK; ++u)
       {
-        if(++spins > SPIN_LIMIT)
-        {
-          atomicOr(err, DEVERR_WAIT);
-          break;
-        }
-        continue;
+        if(done || used < u || k - u < 0) continue;
+        const unsigned flag = v[u] & ~VAL_MASK;
+        if(flag == 0u) continue;
+        excl += v[u] & VAL_MASK;
+        used = u + 1;
+        done = (flag == FLAG_PRE);
       }
-      excl += v & VAL_MASK;
-      if(flag == FLAG_PRE) break;
-      --k;
+      if(done) break;
+      if(used == 0 && ++spins > SPIN_LIMIT)
+      {
+        atomicOr(err, DEVERR_WAIT);
+        break;
+      }
+      k -= used;
     }
     st_volatile(lb, FLAG_PRE | ((excl + total) & VAL_MASK));
   }
