@@ -4,13 +4,15 @@
 // spin/internal/linear_bvh/build_radix_tree.hpp:579-611 and
 // spin/policy/LinearBVH.hpp:191-269):
 //   k_leaf_bounds   scale each box about its midpoint (transform_boxes,
-//                   BR:85-99) and fold the global bounds (reduce, BR:102-143)
-//   k_bounds_final  combine the per-block folds
+//                   BR:85-99) and fold the global bounds (reduce, BR:102-143);
+//                   the last block to finish merges the blocks' folds
 //   k_morton        30-bit Morton code of each scaled box centroid (get_mcodes,
-//                   BR:146-176)
-//   radix sort      stable (key, index) sort (sort_mcodes, BR:225-260)
+//                   BR:146-176), written into the tree's code array
+//   radix sort      stable (key, index) sort (sort_mcodes, BR:225-260) in
+//                   place: four passes end in the tree's code and permutation
+//                   arrays
 //   k_karras        Karras 2012 hierarchy, identical tie-breaking (build_tree,
-//                   BR:265-384)
+//                   BR:265-384); also zeroes the refit's counters
 //   k_refit_persist bottom-up boxes with one atomic per node; the second
 //                   arrival continues (propagate_aabbs, BR:505-576), writing each
 //                   box straight into its parent's 128-byte node record (the
@@ -46,13 +48,31 @@ using lbvh::fold_merge;
 using lbvh::take_max;
 using lbvh::take_min;
 
-// Scaled leaf boxes + per-block folds of the bounds (transform_boxes, BR:85-99,
-// and reduce, BR:102-143).
+// Scaled leaf boxes and the bounds (transform_boxes, BR:85-99, and reduce,
+// BR:102-143): each block folds its boxes and publishes the fold; the last
+// block to finish (one counter, which it resets) merges every block's fold
+// and writes params: bounds lo[3] hi[3], then Morton min[3], inv_extent[3].
+// The merge is commutative (it keeps the leftmost extreme), so the order in
+// which blocks finish does not matter.
+__device__ __forceinline__ Fold load_fold_cg(const Fold* p)
+{
+  Fold f;
+  for(int d = 0; d < 3; ++d)
+  {
+    f.lo[d] = ArgV {__ldcg(&p->lo[d].v), __ldcg(&p->lo[d].i)};
+    f.hi[d] = ArgV {__ldcg(&p->hi[d].v), __ldcg(&p->hi[d].i)};
+  }
+  f.first_valid = __ldcg(&p->first_valid);
+  return f;
+}
+
 __global__ void __launch_bounds__(BUILD_THREADS) k_leaf_bounds(const double* __restrict__ in,
                                                                  int n,
                                                                  double scale,
                                                                  double* __restrict__ leaf,
-                                                                 Fold* __restrict__ partials)
+                                                                 Fold* __restrict__ partials,
+                                                                 int* __restrict__ done,
+                                                                 double* __restrict__ params)
 {
   Fold f;
   fold_init(f);
@@ -73,21 +93,25 @@ __global__ void __launch_bounds__(BUILD_THREADS) k_leaf_bounds(const double* __r
     }
   }
   const Fold a = fold_block(f);
-  if(threadIdx.x == 0) partials[blockIdx.x] = a;
-}
-
-// params: bounds lo[3] hi[3], then Morton min[3], inv_extent[3].
-// One block: the partial folds merged across the block (the merge is
-// commutative: it keeps the leftmost extreme).
-__global__ void __launch_bounds__(BUILD_THREADS) k_bounds_final(const Fold* __restrict__ partials, int nb,
-                                                                  const double* __restrict__ leaf, int n,
-                                                                  double* __restrict__ params)
-{
-  Fold f;
-  fold_init(f);
-  for(int b = threadIdx.x; b < nb; b += blockDim.x) fold_merge(f, partials[b]);
-  const Fold a = fold_block(f);
-  if(threadIdx.x == 0) lbvh::bounds_params(a, leaf, n - 1, params);
+  __shared__ bool s_last;
+  if(threadIdx.x == 0)
+  {
+    partials[blockIdx.x] = a;
+    __threadfence();
+    s_last = (atomicAdd(done, 1) == (int)gridDim.x - 1);
+  }
+  __syncthreads();
+  if(!s_last) return;
+  __threadfence();
+  Fold g;
+  fold_init(g);
+  for(int b = threadIdx.x; b < (int)gridDim.x; b += blockDim.x) fold_merge(g, load_fold_cg(partials + b));
+  const Fold t = fold_block(g);
+  if(threadIdx.x == 0)
+  {
+    lbvh::bounds_params(t, leaf, n - 1, params);
+    *done = 0;
+  }
 }
 
 __global__ void __launch_bounds__(BUILD_THREADS) k_morton(const double* __restrict__ leaf,
@@ -105,10 +129,14 @@ __global__ void __launch_bounds__(BUILD_THREADS) k_karras(const uint32_t* __rest
                                                             int* __restrict__ lchild,
                                                             int* __restrict__ rchild,
                                                             int* __restrict__ parent,
-                                                            NodeRec64* __restrict__ nodes)
+                                                            NodeRec64* __restrict__ nodes,
+                                                            int* __restrict__ counters)
 {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if(i >= n - 1) return;
+  // the refit's node counters and (counters[n - 1]) its work counter
+  counters[i] = 0;
+  if(i == 0) counters[n - 1] = 0;
   lbvh::karras_node(i, codes, n, lchild, rchild, parent, nodes);
 }
 
@@ -198,6 +226,118 @@ __device__ __forceinline__ bool traverse_nopref(const NodeRec64* __restrict__ no
       const int2 ch = __ldg(reinterpret_cast<const int2*>(nodes[cur].child));
       const bool inL = box_valid_k(k, k + 3) ? pred(b, k) : false;
       const bool inR = box_valid_k(k + 6, k + 9) ? pred(b + 6, k + 6) : false;
+      if(!inL && !inR)
+        cur = (sp >= 0) ? todo[sp--] : BARRIER;
+      else
+      {
+        cur = inL ? ch.x : ch.y;
+        if(inL && inR)
+        {
+          if(sp + 1 >= STACK_SIZE) return false;
+          todo[++sp] = ch.y;
+        }
+      }
+      if(cur < 0 && !(found < 0))
+      {
+        found = cur;
+        if(cur != BARRIER) cur = (sp >= 0) ? todo[sp--] : BARRIER;
+      }
+    }
+    while(found < 0 && found != BARRIER)
+    {
+      leaf(-found - 1);
+      found = cur;
+      if(cur < 0 && cur != BARRIER) cur = (sp >= 0) ? todo[sp--] : BARRIER;
+    }
+    found = 0;
+  }
+  return true;
+}
+
+// Comparison keys of a node record's two child boxes (the OKey words of its
+// twelve coordinates, FP64 order as 32-bit integer order), for the box and
+// point finds, whose predicates only compare.  A box is valid when lo <= hi
+// on every axis, so a valid box has no NaN coordinate and its keys need no
+// NaN flag; an invalid box is never entered.  128 bytes per inner node, made
+// from the node records on the first such find after a build: each visit then
+// loads its keys instead of forming them from the doubles.
+struct __align__(16) NodeKeyRec
+{
+  int hi[12];
+  unsigned lo[12];
+  int child[2];
+  int valid;  // bit 0: left box valid, bit 1: right box valid
+  int pad[5];
+};
+static_assert(sizeof(NodeKeyRec) == 128, "key record must be one 128-byte line");
+
+__global__ void __launch_bounds__(BUILD_THREADS) k_node_keys(const NodeRec64* __restrict__ nodes, int inner,
+                                                              NodeKeyRec* __restrict__ out)
+{
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if(i >= inner) return;
+  const double2* r = reinterpret_cast<const double2*>(nodes + i);
+  OKey k[12];
+#pragma unroll
+  for(int j = 0; j < 6; ++j)
+  {
+    const double2 v = __ldg(r + j);
+    k[2 * j] = okey(v.x);
+    k[2 * j + 1] = okey(v.y);
+  }
+  NodeKeyRec o;
+#pragma unroll
+  for(int j = 0; j < 12; ++j)
+  {
+    o.hi[j] = k[j].hi;
+    o.lo[j] = k[j].lo;
+  }
+  const int2 ch = __ldg(reinterpret_cast<const int2*>(nodes[i].child));
+  o.child[0] = ch.x;
+  o.child[1] = ch.y;
+  o.valid = (box_valid_k(k, k + 3) ? 1 : 0) | (box_valid_k(k + 6, k + 9) ? 2 : 0);
+  for(int j = 0; j < 5; ++j) o.pad[j] = 0;
+  int4* dst = reinterpret_cast<int4*>(out + i);
+  const int4* src = reinterpret_cast<const int4*>(&o);
+#pragma unroll
+  for(int j = 0; j < 8; ++j) dst[j] = src[j];
+}
+
+// traverse_nopref over the key records: the same visits, leaves and order.
+template <class Pred, class Leaf>
+__device__ __forceinline__ bool traverse_keys(const NodeKeyRec* __restrict__ nk, Pred& pred, Leaf& leaf)
+{
+  int todo[STACK_SIZE];
+  int sp = 0;
+  todo[0] = BARRIER;
+  int found = 0, cur = 0;
+  while(cur != BARRIER)
+  {
+    while(cur >= 0)
+    {
+      const int4* r = reinterpret_cast<const int4*>(nk + cur);
+      int w[28];
+#pragma unroll
+      for(int j = 0; j < 7; ++j)
+      {
+        const int4 v = __ldg(r + j);
+        w[4 * j] = v.x;
+        w[4 * j + 1] = v.y;
+        w[4 * j + 2] = v.z;
+        w[4 * j + 3] = v.w;
+      }
+      OKey k[12];
+#pragma unroll
+      for(int j = 0; j < 12; ++j)
+      {
+        k[j].hi = w[j];
+        k[j].lo = (unsigned)w[12 + j];
+        k[j].nan = false;
+      }
+      const int2 ch = make_int2(w[24], w[25]);
+      const int valid = w[26];
+      const bool inL = (valid & 1) ? pred(nullptr, k) : false;
+      const bool inR = (valid & 2) ? pred(nullptr, k + 6) : false;
       if(!inL && !inR)
         cur = (sp >= 0) ? todo[sp--] : BARRIER;
       else
@@ -342,8 +482,21 @@ __device__ __forceinline__ auto make_query(const QueryArgs& q, int i)
 constexpr int FIND_THREADS = 128;
 constexpr int FIND_CAP = 8;  // candidates kept per query by pass 1
 
+// Boxes and points traverse the key records, rays the node records (their
+// slab test needs the coordinates).
+template <int KIND, class Pred, class Leaf>
+__device__ __forceinline__ bool find_traverse(const NodeRec64* __restrict__ nodes, const NodeKeyRec* __restrict__ nk,
+                                              Pred& pred, Leaf& leaf)
+{
+  if constexpr(KIND == Q_RAYS)
+    return traverse_nopref(nodes, pred, leaf);
+  else
+    return traverse_keys(nk, pred, leaf);
+}
+
 template <int KIND>
 __global__ void __launch_bounds__(FIND_THREADS) k_find_pass1(const NodeRec64* __restrict__ nodes,
+                                                               const NodeKeyRec* __restrict__ nk,
                                                                const int* __restrict__ perm,
                                                                QueryArgs qa,
                                                                int m,
@@ -360,12 +513,13 @@ __global__ void __launch_bounds__(FIND_THREADS) k_find_pass1(const NodeRec64* __
     if(c < FIND_CAP) mine[c] = __ldg(perm + leafpos);
     ++c;
   };
-  if(!traverse_nopref(nodes, pred, leaf)) atomicOr(err, DEVERR_STACK);
+  if(!find_traverse<KIND>(nodes, nk, pred, leaf)) atomicOr(err, DEVERR_STACK);
   counts[i] = c;
 }
 
 template <int KIND>
 __global__ void __launch_bounds__(FIND_THREADS) k_find_pass2(const NodeRec64* __restrict__ nodes,
+                                                               const NodeKeyRec* __restrict__ nk,
                                                                const int* __restrict__ perm,
                                                                QueryArgs qa,
                                                                int m,
@@ -389,7 +543,7 @@ __global__ void __launch_bounds__(FIND_THREADS) k_find_pass2(const NodeRec64* __
     if(w < c) out[w] = __ldg(perm + leafpos);
     ++w;
   };
-  traverse_nopref(nodes, pred, leaf);
+  find_traverse<KIND>(nodes, nk, pred, leaf);
 }
 
 inline int grid_for(long long n, int threads) { return (int)std::max<long long>(1, (n + threads - 1) / threads); }
@@ -480,11 +634,13 @@ void BvhDev::release()
 
 namespace
 {
-size_t align256(size_t x) { return (x + 255) & ~size_t(255); }
 
 // Scratch of one build over n boxes.
+constexpr size_t BUILD_FIXED_BYTES = 256;
+
 struct BuildScratch
 {
+  int* fold_done;
   double* leaf;
   double* params;
   uint32_t* keys[2];
@@ -508,10 +664,14 @@ size_t build_scratch_layout(int n, char* base, BuildScratch* out)
   const size_t sz_cnt = align256(sizeof(int) * (inner + 1));  // node counters, then the refit's work counter
   const size_t sz_fold = align256(sizeof(Fold) * fold_blocks);
   const size_t sz_sort = align256(radix_sort_work_bytes(n));
-  const size_t total = sz_leaf + sz_params + 4 * sz_u32 + sz_par + sz_cnt + sz_fold + sz_sort;
+  // the first 256 bytes hold words whose place does not depend on n: the
+  // bounds fold's block counter (zeroed once when the scratch is allocated;
+  // the last block of every build resets it)
+  const size_t total = BUILD_FIXED_BYTES + sz_leaf + sz_params + 4 * sz_u32 + sz_par + sz_cnt + sz_fold + sz_sort;
   if(out)
   {
-    char* w = base;
+    out->fold_done = reinterpret_cast<int*>(base);
+    char* w = base + BUILD_FIXED_BYTES;
     out->leaf = reinterpret_cast<double*>(w);
     w += sz_leaf;
     out->params = reinterpret_cast<double*>(w);
@@ -542,18 +702,22 @@ int enqueue_build(BvhDev& B, const BuildScratch& w, const double* d_boxes, int n
                   int* d_err)
 {
   const int inner = n - 1;
-  k_leaf_bounds<<<w.fold_blocks, BUILD_THREADS, 0, s>>>(d_boxes, n, scale, w.leaf, w.folds);
-  k_bounds_final<<<1, BUILD_THREADS, 0, s>>>(w.folds, w.fold_blocks, w.leaf, n, w.params);
-  k_morton<<<grid_for(n, BUILD_THREADS), BUILD_THREADS, 0, s>>>(w.leaf, n, w.params, w.keys[0]);
-  count_launch(3);
-  uint32_t* keys[2] = {w.keys[0], w.keys[1]};
-  int* vals[2] = {w.vals[0], w.vals[1]};
+  k_leaf_bounds<<<w.fold_blocks, BUILD_THREADS, 0, s>>>(d_boxes, n, scale, w.leaf, w.folds, w.fold_done, w.params);
+  // the codes and the permutation are sorted in place into the tree's arrays
+  // (four passes end in the first buffer)
+  k_morton<<<grid_for(n, BUILD_THREADS), BUILD_THREADS, 0, s>>>(w.leaf, n, w.params, B.codes);
+  count_launch(2);
+  uint32_t* keys[2] = {B.codes, w.keys[1]};
+  int* vals[2] = {B.perm, w.vals[1]};
   const int which = radix_sort_pairs_prealloc(keys, vals, n, 30, true, w.sort_work, w.sort_bytes, s, d_err);
   if(which < 0) return which;
-  GSQ_CUDA_TRY(cudaMemcpyAsync(B.codes, keys[which], sizeof(uint32_t) * n, cudaMemcpyDeviceToDevice, s));
-  GSQ_CUDA_TRY(cudaMemcpyAsync(B.perm, vals[which], sizeof(int) * n, cudaMemcpyDeviceToDevice, s));
-  k_karras<<<grid_for(inner, BUILD_THREADS), BUILD_THREADS, 0, s>>>(B.codes, n, B.lchild, B.rchild, w.parent, B.nodes);
-  GSQ_CUDA_TRY(cudaMemsetAsync(w.counters, 0, sizeof(int) * (inner + 1), s));
+  if(which != 0)
+  {
+    GSQ_CUDA_TRY(cudaMemcpyAsync(B.codes, keys[which], sizeof(uint32_t) * n, cudaMemcpyDeviceToDevice, s));
+    GSQ_CUDA_TRY(cudaMemcpyAsync(B.perm, vals[which], sizeof(int) * n, cudaMemcpyDeviceToDevice, s));
+  }
+  k_karras<<<grid_for(inner, BUILD_THREADS), BUILD_THREADS, 0, s>>>(B.codes, n, B.lchild, B.rchild, w.parent, B.nodes,
+                                                                   w.counters);
   int dev = 0, sms = 0, per_sm = 0;
   GSQ_CUDA_TRY(cudaGetDevice(&dev));
   GSQ_CUDA_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
@@ -567,7 +731,7 @@ int enqueue_build(BvhDev& B, const BuildScratch& w, const double* d_boxes, int n
 }
 }  // namespace
 
-int bvh_build(BvhDev& B, const double* d_boxes, int n, double scale, cudaStream_t s, int* d_err)
+int bvh_build(BvhDev& B, const double* d_boxes, int n, double scale, cudaStream_t s, int* d_err, cudaEvent_t done)
 {
   if(n < 0) return fail(GSQ_ERR_INVALID, "number of boxes must be >= 0");
   // BVH::initialize (spin/BVH.hpp:436-463): 0 or 1 boxes -> 2, second invalid.
@@ -612,6 +776,7 @@ int bvh_build(BvhDev& B, const double* d_boxes, int n, double scale, cudaStream_
     B.work_bytes = 0;
     GSQ_CUDA_TRY(cudaMalloc(&B.work, wbytes));
     B.work_bytes = wbytes;
+    GSQ_CUDA_TRY(cudaMemsetAsync(B.work, 0, BUILD_FIXED_BYTES, s));
   }
   char* base = static_cast<char*>(B.block);
   B.n = n;
@@ -666,6 +831,7 @@ int bvh_build(BvhDev& B, const double* d_boxes, int n, double scale, cudaStream_
     GSQ_CUDA_TRY(cudaGraphLaunch(B.exec, s));
     count_launch(B.graph_kernels);
   }
+  if(done) GSQ_CUDA_TRY(cudaEventRecord(done, s));
   GSQ_CUDA_TRY(cudaMemcpyAsync(B.bounds, w.params, sizeof(double) * 6, cudaMemcpyDeviceToHost, s));
   GSQ_CUDA_TRY(cudaStreamSynchronize(s));
   return check_device_error(d_err, s, "bvh build");
@@ -714,6 +880,13 @@ struct gsq_bvh
   mutable float find_ms = 0.f;  // device time of the last find's two passes and scan
   mutable FindCache fc;
   int* d_err = nullptr;
+  // the key records of the box and point finds: made by the first such find
+  // after a build (under nk_mu; nk_ev orders later finds on other streams)
+  mutable gsq::NodeKeyRec* nkeys = nullptr;
+  mutable size_t nkeys_cap = 0;
+  mutable bool nkeys_ok = false;
+  mutable std::mutex nk_mu;
+  mutable cudaEvent_t nk_ev = nullptr;
 };
 
 namespace
@@ -722,6 +895,34 @@ int check_bvh(const gsq_bvh* h)
 {
   if(!h) return fail(GSQ_ERR_INVALID, "null bvh handle");
   if(!h->built) return fail(GSQ_ERR_STATE, "bvh has not been built");
+  return GSQ_OK;
+}
+
+// The key records of the current tree, made on stream s if the tree has none.
+int node_keys(const gsq_bvh* h, cudaStream_t s, const NodeKeyRec** out)
+{
+  std::lock_guard<std::mutex> g(h->nk_mu);
+  const int inner = h->dev.n - 1;
+  if(!h->nkeys_ok)
+  {
+    if((size_t)inner > h->nkeys_cap)
+    {
+      if(h->nkeys) cudaFree(h->nkeys);
+      h->nkeys = nullptr;
+      h->nkeys_cap = 0;
+      GSQ_CUDA_TRY(cudaMalloc(&h->nkeys, sizeof(NodeKeyRec) * (size_t)inner));
+      h->nkeys_cap = (size_t)inner;
+    }
+    if(!h->nk_ev) GSQ_CUDA_TRY(cudaEventCreateWithFlags(&h->nk_ev, cudaEventDisableTiming));
+    count_launch();
+    k_node_keys<<<grid_for(inner, BUILD_THREADS), BUILD_THREADS, 0, s>>>(h->dev.nodes, inner, h->nkeys);
+    GSQ_CUDA_TRY(cudaGetLastError());
+    GSQ_CUDA_TRY(cudaEventRecord(h->nk_ev, s));
+    h->nkeys_ok = true;
+  }
+  else
+    GSQ_CUDA_TRY(cudaStreamWaitEvent(s, h->nk_ev, 0));
+  *out = h->nkeys;
   return GSQ_OK;
 }
 
@@ -787,11 +988,17 @@ int find_impl(const gsq_bvh* h, const double* a, const double* b, int32_t m, int
   int* d_cnt = static_cast<int*>(cnt_buf.dev);
   int* d_off = static_cast<int*>(off_buf.dev);
   cudaEventRecord(ev[0], s);
+  const NodeKeyRec* nk = nullptr;
+  if(KIND != Q_RAYS && m > 0)
+  {
+    rc = node_keys(h, s, &nk);
+    if(rc) return rc;
+  }
   if(m > 0)
   {
     count_launch();
-    k_find_pass1<KIND><<<grid_for(m, FIND_THREADS), FIND_THREADS, 0, s>>>(h->dev.nodes, h->dev.perm, qa, m, d_cnt,
-                                                                          keep, h->d_err);
+    k_find_pass1<KIND><<<grid_for(m, FIND_THREADS), FIND_THREADS, 0, s>>>(h->dev.nodes, nk, h->dev.perm, qa, m,
+                                                                          d_cnt, keep, h->d_err);
   }
   rc = exclusive_scan(d_cnt, d_off, m, d_tot, s, scan_work);
   if(rc) return rc;
@@ -814,8 +1021,8 @@ int find_impl(const gsq_bvh* h, const double* a, const double* b, int32_t m, int
   if(m > 0)
   {
     count_launch();
-    k_find_pass2<KIND><<<grid_for(m, FIND_THREADS), FIND_THREADS, 0, s>>>(h->dev.nodes, h->dev.perm, qa, m, d_cnt,
-                                                                          d_off, keep, d_cand);
+    k_find_pass2<KIND><<<grid_for(m, FIND_THREADS), FIND_THREADS, 0, s>>>(h->dev.nodes, nk, h->dev.perm, qa, m,
+                                                                          d_cnt, d_off, keep, d_cand);
   }
   cudaEventRecord(ev[3], s);
   cudaError_t e = cudaGetLastError();
@@ -882,6 +1089,8 @@ int gsq_bvh_destroy(gsq_bvh* h)
   if(!h) return GSQ_OK;
   h->dev.release();
   h->fc.release();
+  if(h->nkeys) cudaFree(h->nkeys);
+  if(h->nk_ev) cudaEventDestroy(h->nk_ev);
   if(h->d_err) cudaFree(h->d_err);
   delete h;
   return GSQ_OK;
@@ -919,6 +1128,7 @@ int gsq_bvh_build(gsq_bvh* h, const double* boxes, int32_t n, void* stream)
   if(n >= (1 << 30)) return fail(GSQ_ERR_INVALID, "at most 2^30-1 boxes");
   cudaStream_t s = static_cast<cudaStream_t>(stream);
   h->built = false;
+  h->nkeys_ok = false;
   // host boxes go to a staging buffer kept with the handle, so that a repeated
   // build from the same host array replays the captured build
   const double* d_boxes = boxes;
@@ -940,9 +1150,10 @@ int gsq_bvh_build(gsq_bvh* h, const double* boxes, int32_t n, void* stream)
   cudaEvent_t e0, e1;
   GSQ_CUDA_TRY(cudaEventCreate(&e0));
   GSQ_CUDA_TRY(cudaEventCreate(&e1));
+  // device time of the build's work: e1 is recorded once it is enqueued,
+  // before the read-back of the bounds and of the error word
   cudaEventRecord(e0, s);
-  const int rc = bvh_build(h->dev, d_boxes, n, h->scale, s, h->d_err);
-  cudaEventRecord(e1, s);
+  const int rc = bvh_build(h->dev, d_boxes, n, h->scale, s, h->d_err, e1);
   cudaEventSynchronize(e1);
   cudaEventElapsedTime(&h->build_ms, e0, e1);
   cudaEventDestroy(e0);
@@ -1056,6 +1267,7 @@ gsq_bvh* bvh_new_internal(int device)
 int bvh_build_internal(gsq_bvh* h, const double* d_boxes, int n, cudaStream_t s)
 {
   h->built = false;
+  h->nkeys_ok = false;
   const int rc = bvh_build(h->dev, d_boxes, n, h->scale, s, h->d_err);
   if(rc == GSQ_OK) h->built = true;
   return rc;

@@ -98,17 +98,23 @@ struct InBuf
 {
   const void* dev = nullptr;
   Scratch own;
-  cudaError_t stage(const void* user, size_t bytes, cudaStream_t s)
+  // ext: device memory of at least `bytes` to stage into (else allocated)
+  cudaError_t stage(const void* user, size_t bytes, cudaStream_t s, void* ext = nullptr)
   {
     if(user == nullptr || bytes == 0 || is_device_ptr(user))
     {
       dev = user;
       return cudaSuccess;
     }
-    cudaError_t e = own.alloc(bytes, s);
-    if(e != cudaSuccess) return e;
-    dev = own.p;
-    return cudaMemcpyAsync(own.p, user, bytes, cudaMemcpyHostToDevice, s);
+    void* d = ext;
+    if(!d)
+    {
+      cudaError_t e = own.alloc(bytes, s);
+      if(e != cudaSuccess) return e;
+      d = own.p;
+    }
+    dev = d;
+    return cudaMemcpyAsync(d, user, bytes, cudaMemcpyHostToDevice, s);
   }
 };
 
@@ -119,13 +125,19 @@ struct OutBuf
   void* dev = nullptr;
   size_t bytes = 0;
   Scratch own;
-  cudaError_t prepare(void* u, size_t b, cudaStream_t s)
+  // ext: device memory of at least `b` to use for a host output (else allocated)
+  cudaError_t prepare(void* u, size_t b, cudaStream_t s, void* ext = nullptr)
   {
     user = u;
     bytes = b;
     if(u == nullptr || b == 0 || is_device_ptr(u))
     {
       dev = u;
+      return cudaSuccess;
+    }
+    if(ext)
+    {
+      dev = ext;
       return cudaSuccess;
     }
     cudaError_t e = own.alloc(b, s);
@@ -196,8 +208,11 @@ struct BvhDev
 };
 
 // Builds the hierarchy over n boxes (device array, n x 6), padding 0/1 boxes
-// to 2 like BVH::initialize.  Returns a GSQ status.
-int bvh_build(BvhDev& B, const double* d_boxes, int n, double scale, cudaStream_t s, int* d_err);
+// to 2 like BVH::initialize.  `done`, when given, is recorded on s once the
+// build's device work is enqueued (before the bounds are read back).  Returns
+// a GSQ status.
+int bvh_build(BvhDev& B, const double* d_boxes, int n, double scale, cudaStream_t s, int* d_err,
+              cudaEvent_t done = nullptr);
 
 // Stable LSD radix sort of (key, value) pairs on key bits [0, end_bit).
 // Inputs in keys[0]/vals[0]; keys[1]/vals[1] are scratch of the same size.
@@ -210,6 +225,8 @@ int radix_sort_pairs(uint32_t* keys[2], int* vals[2], int n, int end_bit, bool v
 // The same sort with a caller-provided workspace of at least
 // radix_sort_work_bytes(n) bytes (no allocation).
 size_t radix_sort_work_bytes(int n);
+// x rounded up to a multiple of 256 bytes
+inline size_t align256(size_t x) { return (x + 255) & ~size_t(255); }
 int radix_sort_pairs_prealloc(uint32_t* keys[2], int* vals[2], int n, int end_bit, bool vals_iota, void* work,
                               size_t work_bytes, cudaStream_t s, int* d_err);
 

@@ -183,29 +183,47 @@ void sdf_release(gsq_sdf* h)
   if(h->leaves32) cudaFree(h->leaves32);
   if(h->d_audit) cudaFree(h->d_audit);
   if(h->d_work) cudaFree(h->d_work);
+  if(h->eval_buf) cudaFree(h->eval_buf);
   if(h->d_mesh) cudaFree(h->d_mesh);
   if(h->d_err) cudaFree(h->d_err);
   if(h->bvh) gsq_bvh_destroy(h->bvh);
   delete h;
 }
 
+// Bytes of device memory the staged query coordinates take: one block of
+// 3m doubles for interleaved points, else one span per coordinate array kept
+// in host memory.  ext (optional) is where stage_queries puts them.
+size_t stage_query_bytes(const double* qx, const double* qy, const double* qz, int stride, int m)
+{
+  const size_t span = align256(sizeof(double) * ((size_t)(m - 1) * stride + 1));
+  if(stride == 3 && qy == qx + 1 && qz == qx + 2) return is_device_ptr(qx) ? 0 : align256(sizeof(double) * 3 * (size_t)m);
+  size_t b = 0;
+  for(const double* a : {qx, qy, qz})
+    if(!is_device_ptr(a)) b += span;
+  return b;
+}
+
 int stage_queries(const double* qx, const double* qy, const double* qz, int stride, int m, cudaStream_t s,
-                  InBuf* bufs, QueryPts& qp)
+                  InBuf* bufs, QueryPts& qp, char* ext = nullptr)
 {
   qp.stride = stride;
   const size_t span = sizeof(double) * ((size_t)(m - 1) * stride + 1);
   const bool aos = (stride == 3 && qy == qx + 1 && qz == qx + 2);
   if(aos)
   {
-    GSQ_CUDA_TRY(bufs[0].stage(qx, sizeof(double) * 3 * (size_t)m, s));
+    GSQ_CUDA_TRY(bufs[0].stage(qx, sizeof(double) * 3 * (size_t)m, s, ext));
     qp.x = static_cast<const double*>(bufs[0].dev);
     qp.y = qp.x + 1;
     qp.z = qp.x + 2;
     return GSQ_OK;
   }
-  GSQ_CUDA_TRY(bufs[0].stage(qx, span, s));
-  GSQ_CUDA_TRY(bufs[1].stage(qy, span, s));
-  GSQ_CUDA_TRY(bufs[2].stage(qz, span, s));
+  const double* src[3] = {qx, qy, qz};
+  for(int k = 0; k < 3; ++k)
+  {
+    char* e = (ext && !is_device_ptr(src[k])) ? ext : nullptr;
+    GSQ_CUDA_TRY(bufs[k].stage(src[k], span, s, e));
+    if(e) ext += align256(span);
+  }
   qp.x = static_cast<const double*>(bufs[0].dev);
   qp.y = static_cast<const double*>(bufs[1].dev);
   qp.z = static_cast<const double*>(bufs[2].dev);
@@ -415,24 +433,61 @@ int gsq_sdf_eval(const gsq_sdf* hc, const double* qx, const double* qy, const do
   if(m == 0) return GSQ_OK;
   if(!qx || !qy || !qz || !out) return fail(GSQ_ERR_INVALID, "null query or output array");
   cudaStream_t s = static_cast<cudaStream_t>(stream);
+  // Staging of host points and outputs, the sort's buffers and the persistent
+  // kernel's work counter: the handle's (grow-only), held until this call has
+  // synchronised its stream below, or the call's own when another thread is
+  // evaluating on this handle (computeDistances is const and re-entrant).
+  std::unique_lock<std::mutex> lock(h->work_busy, std::try_to_lock);
+  const bool cached = lock.owns_lock();
+  const bool sort = h->opts.sort_queries && m > 1;
+  const size_t in_bytes = stage_query_bytes(qx, qy, qz, stride, m);
+  const size_t out_bytes[3] = {is_device_ptr(out) ? 0 : align256(sizeof(double) * (size_t)m),
+                               (!closest || is_device_ptr(closest)) ? 0 : align256(sizeof(double) * 3 * (size_t)m),
+                               (!normals || is_device_ptr(normals)) ? 0 : align256(sizeof(double) * 3 * (size_t)m)};
+  const size_t order_bytes = sort ? align256(4 * sizeof(uint32_t) * (size_t)m) : 0;
+  const size_t sort_bytes = sort ? align256(radix_sort_work_bytes(m)) : 0;
+  char* cv = nullptr;
+  if(cached)
+  {
+    const size_t need = in_bytes + out_bytes[0] + out_bytes[1] + out_bytes[2] + order_bytes + sort_bytes;
+    if(need > h->eval_bytes)
+    {
+      if(h->eval_buf) cudaFree(h->eval_buf);
+      h->eval_buf = nullptr;
+      h->eval_bytes = 0;
+      GSQ_CUDA_TRY(cudaMalloc(&h->eval_buf, need));
+      h->eval_bytes = need;
+    }
+    cv = static_cast<char*>(h->eval_buf);
+  }
+  auto take = [&](size_t b) -> char* {
+    if(!cv || b == 0) return nullptr;
+    char* r = cv;
+    cv += b;
+    return r;
+  };
   InBuf qb[3];
   QueryPts qp;
-  int rc = stage_queries(qx, qy, qz, stride, m, s, qb, qp);
+  int rc = stage_queries(qx, qy, qz, stride, m, s, qb, qp, take(in_bytes));
   if(rc) return rc;
   OutBuf ob, cb, nb;
-  GSQ_CUDA_TRY(ob.prepare(out, sizeof(double) * (size_t)m, s));
-  GSQ_CUDA_TRY(cb.prepare(closest, sizeof(double) * 3 * (size_t)m, s));
-  GSQ_CUDA_TRY(nb.prepare(normals, sizeof(double) * 3 * (size_t)m, s));
+  GSQ_CUDA_TRY(ob.prepare(out, sizeof(double) * (size_t)m, s, take(out_bytes[0])));
+  GSQ_CUDA_TRY(cb.prepare(closest, sizeof(double) * 3 * (size_t)m, s, take(out_bytes[1])));
+  GSQ_CUDA_TRY(nb.prepare(normals, sizeof(double) * 3 * (size_t)m, s, take(out_bytes[2])));
 
   const BvhDev* B = bvh_dev(h->bvh);
   Scratch order_buf;
   const int* order = nullptr;
-  if(h->opts.sort_queries && m > 1)
+  if(sort)
   {
-    GSQ_CUDA_TRY(order_buf.alloc(4 * sizeof(uint32_t) * (size_t)m, s));
-    uint32_t* keys[2] = {order_buf.as<uint32_t>(), order_buf.as<uint32_t>() + m};
-    int* vals[2] = {reinterpret_cast<int*>(order_buf.as<uint32_t>() + 2 * (size_t)m),
-                    reinterpret_cast<int*>(order_buf.as<uint32_t>() + 3 * (size_t)m)};
+    uint32_t* ob4 = reinterpret_cast<uint32_t*>(take(order_bytes));
+    if(!ob4)
+    {
+      GSQ_CUDA_TRY(order_buf.alloc(4 * sizeof(uint32_t) * (size_t)m, s));
+      ob4 = order_buf.as<uint32_t>();
+    }
+    uint32_t* keys[2] = {ob4, ob4 + m};
+    int* vals[2] = {reinterpret_cast<int*>(ob4 + 2 * (size_t)m), reinterpret_cast<int*>(ob4 + 3 * (size_t)m)};
     const double* b = B->bounds;
     double sc[3];
     for(int d = 0; d < 3; ++d)
@@ -442,7 +497,9 @@ int gsq_sdf_eval(const gsq_sdf* hc, const double* qx, const double* qy, const do
     }
     count_launch();
     k_query_codes<<<grid_for(m, 256), 256, 0, s>>>(qp, m, b[0], b[1], b[2], sc[0], sc[1], sc[2], keys[0]);
-    const int which = radix_sort_pairs(keys, vals, m, 30, true, s, h->d_err);
+    char* sw = take(sort_bytes);
+    const int which = sw ? radix_sort_pairs_prealloc(keys, vals, m, 30, true, sw, sort_bytes, s, h->d_err)
+                         : radix_sort_pairs(keys, vals, m, 30, true, s, h->d_err);
     if(which < 0) return which;
     order = vals[which];
   }
@@ -459,15 +516,11 @@ int gsq_sdf_eval(const gsq_sdf* hc, const double* qx, const double* qy, const do
   const bool audit = mixed && h->opts.audit;
   if(audit) GSQ_CUDA_TRY(cudaMemsetAsync(h->d_audit, 0, 4 * sizeof(unsigned long long), s));
   cudaEventRecord(e0, s);
-  // the persistent kernel's work counter: the handle's, held until this call
-  // has synchronised its stream below, or the call's own when another thread
-  // is evaluating on this handle (computeDistances is const and re-entrant)
-  std::unique_lock<std::mutex> work_lock(h->work_busy, std::defer_lock);
   Scratch own_work;
   if(mixed)
   {
     int* work = h->d_work;
-    if(!work_lock.try_lock())
+    if(!cached)
     {
       GSQ_CUDA_TRY(own_work.alloc(sizeof(int), s));
       work = own_work.as<int>();

@@ -29,7 +29,9 @@ struct gsq_sdf
   float mesh_max = 0.f;          // max |coordinate| of the mesh, rounded up
   unsigned long long* d_audit = nullptr;
   int* d_work = nullptr;          // work-queue counter of the persistent query kernel
-  std::mutex work_busy;           // held by the evaluation using d_work
+  std::mutex work_busy;           // held by the evaluation using d_work and eval_buf
+  void* eval_buf = nullptr;       // an evaluation's staging and sort scratch (grow-only)
+  size_t eval_bytes = 0;
   gsq::MeshInfo* d_mesh = nullptr; // the single mesh's entry for the query kernel
   long long audit[4] = {0, 0, 0, 0};
   int* d_err = nullptr;

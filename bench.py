@@ -566,8 +566,11 @@ def run_gsq(args, world, rank, local):
     clocks_e2e = Clocks(local)
     clocks_e2e.start()
     t0 = time.perf_counter()
+    e2e_steps = []
     for _ in range(args.steps):
+        t1 = time.perf_counter()
         sd.compute_distances(q_pin, out=out_pin)
+        e2e_steps.append((time.perf_counter() - t1) * 1000.0)
     barrier()
     e2e_ms = max_over_ranks((time.perf_counter() - t0) * 1000.0 / args.steps)
     clk_e2e = clocks_e2e.stop()
@@ -613,7 +616,8 @@ def run_gsq(args, world, rank, local):
                      "kernel_ms": kernel_ms,
                      "algorithmic_bytes_per_query": bq, "box_tests_per_query": nb, "leaf_tests_per_query": nl},
         "e2e": {"value": world * m / (e2e_ms / 1000.0), "unit": UNIT, "ms_per_step": e2e_ms,
-                "h2d_bytes_per_step": 24 * m, "d2h_bytes_per_step": 8 * m, "clocks": clk_e2e},
+                "h2d_bytes_per_step": 24 * m, "d2h_bytes_per_step": 8 * m, "clocks": clk_e2e,
+                "step_ms_min_median_max": [min(e2e_steps), statistics.median(e2e_steps), max(e2e_steps)]},
         "gpu_launches": int(launches),
         "clocks": clk,
     }
