@@ -557,11 +557,21 @@ def run_gsq(args, world, rank, local):
 
     # End to end through the public API with host buffers: pinned host points in,
     # pinned host distances out, copies inside the timed region (measured right
-    # after the device-resident steps, before the long FP64 leg heats the GPU).
+    # after the device-resident steps, before the FP64 leg).
     q_pin = torch.from_numpy(q_host).pin_memory()
     out_pin = torch.empty(m, dtype=torch.float64).pin_memory()
     for _ in range(max(1, args.warmup)):
         sd.compute_distances(q_pin, out=out_pin)
+    # the host link's copy rates at this moment (the GPUs of a machine share
+    # their hosts' memory, so other jobs can slow these copies)
+    link = {}
+    for name, dst, src in (("h2d_gbs", q_dev, q_pin), ("d2h_gbs", out_pin, out)):
+        dst.copy_(src, non_blocking=True)
+        torch.cuda.synchronize()
+        t1 = time.perf_counter()
+        dst.copy_(src, non_blocking=True)
+        torch.cuda.synchronize()
+        link[name] = src.numel() * src.element_size() / (time.perf_counter() - t1) / 1e9
     barrier()
     clocks_e2e = Clocks(local)
     clocks_e2e.start()
@@ -617,7 +627,8 @@ def run_gsq(args, world, rank, local):
                      "algorithmic_bytes_per_query": bq, "box_tests_per_query": nb, "leaf_tests_per_query": nl},
         "e2e": {"value": world * m / (e2e_ms / 1000.0), "unit": UNIT, "ms_per_step": e2e_ms,
                 "h2d_bytes_per_step": 24 * m, "d2h_bytes_per_step": 8 * m, "clocks": clk_e2e,
-                "step_ms_min_median_max": [min(e2e_steps), statistics.median(e2e_steps), max(e2e_steps)]},
+                "step_ms_min_median_max": [min(e2e_steps), statistics.median(e2e_steps), max(e2e_steps)],
+                "link": link},
         "gpu_launches": int(launches),
         "clocks": clk,
     }
