@@ -10,15 +10,17 @@
 //   dd/dq  =  s u                 dd/dV_k = -s b_k u
 // (the sign is piecewise constant; at |q - cp| = 0 both are taken as 0).
 //
-// k_sdf_adjoint recomputes each point's closest triangle with the same
-// certified traversal as the mixed form (so cp is the forward's cp bit for bit)
-// and writes dL/dq plus three vertex contributions per point.  The vertex
+// The backward pass runs the persistent mixed query (the forward's traversal,
+// so cp is the forward's cp bit for bit), which also writes each point's
+// closest triangle; k_adjoint_apply then forms cp's barycentric weights on
+// that triangle and writes dL/dq plus three vertex contributions per point,
+// the sign taken from the signed distance the query wrote.  The vertex
 // gradient is then reduced deterministically: the contributions are sorted by
 // vertex id with a stable radix sort (ties keep point order) and each vertex's
 // segment is summed by one thread in that order, so the result does not depend
 // on scheduling and repeats bit for bit.
 #include "gsq_sdf_handle.cuh"
-#include "gsq_sdf_mixed.cuh"
+#include "gsq_sdf_mixed_kernel.cuh"
 
 #include <algorithm>
 #include <cstring>
@@ -95,70 +97,34 @@ __device__ __forceinline__ void closest_point_bary(const double* P, const double
   bary[0] = 1.0 - v - w, bary[1] = v, bary[2] = w;
 }
 
-// The sign the forward pass gives the point (SD:583-592).
+// Per point: the gradient directions from its closest triangle (leaf code
+// from the mixed query: leaf position * 2 + triangle, -1 for none) and the
+// sign of its signed distance d = sqrt(minSq) * sign.
 template <int NPC>
-__device__ __forceinline__ double query_sign(const double* q, const MinCand& mc, const LeafRec<NPC>* __restrict__ leaves,
-                                             const SdfParams& prm)
+__global__ void __launch_bounds__(256) k_adjoint_apply(const LeafRec<NPC>* __restrict__ leaves64,
+                                                       const int* __restrict__ cells,
+                                                       QueryPts qp,
+                                                       int m,
+                                                       const double* __restrict__ dist,
+                                                       const int* __restrict__ leaf_code,
+                                                       const double* __restrict__ grad_d,
+                                                       double* __restrict__ grad_q,
+                                                       uint32_t* __restrict__ vkeys,
+                                                       double* __restrict__ vcontrib)
 {
-  if(!prm.sign) return 1.0;
-  const double* D = prm.domain;
-  const bool inside_box = !(mc.mp[0] < D[0] || mc.mp[0] > D[3] || mc.mp[1] < D[1] || mc.mp[1] > D[4] ||
-                            mc.mp[2] < D[2] || mc.mp[2] > D[5]);
-  if(prm.watertight && !inside_box) return 1.0;
-  double nrm[3] = {mc.sn[0], mc.sn[1], mc.sn[2]};
-  if(mc.type == 2)
-  {
-    double v[3 * NPC];
-    load_leaf<NPC>(leaves, mc.leaf, v);
-    if(NPC == 4 && mc.sub == 1)
-      tri_normal(v, v + 6, v + 9, nrm);
-    else
-      tri_normal(v, v + 3, v + 6, nrm);
-  }
-  else if(mc.npend > 0)
-  {
-    MinCand m = mc;
-    flush_normals<NPC>(m, leaves);
-    nrm[0] = m.sn[0], nrm[1] = m.sn[1], nrm[2] = m.sn[2];
-  }
-  const double r0 = q[0] - mc.mp[0], r1 = q[1] - mc.mp[1], r2 = q[2] - mc.mp[2];
-  return (dot3(r0, r1, r2, nrm[0], nrm[1], nrm[2]) >= 0.0) ? 1.0 : -1.0;
-}
-
-template <int NPC>
-__global__ void __launch_bounds__(128) k_sdf_adjoint(const NodeRec64* __restrict__ nodes64,
-                                                     const NodeRec32* __restrict__ nodes32,
-                                                     const LeafRec<NPC>* __restrict__ leaves64,
-                                                     const LeafRec32<NPC>* __restrict__ leaves32,
-                                                     const int* __restrict__ cells,
-                                                     QueryPts qp,
-                                                     int m,
-                                                     const int* __restrict__ order,
-                                                     SdfParams prm,
-                                                     float mesh_max,
-                                                     const double* __restrict__ grad_d,
-                                                     double* __restrict__ grad_q,
-                                                     uint32_t* __restrict__ vkeys,
-                                                     double* __restrict__ vcontrib,
-                                                     int* err)
-{
-  const int t = blockIdx.x * blockDim.x + threadIdx.x;
-  if(t >= m) return;
-  const int idx = order ? __ldg(order + t) : t;
+  const int idx = blockIdx.x * blockDim.x + threadIdx.x;
+  if(idx >= m) return;
   const double q[3] = {qp.x[(size_t)idx * qp.stride], qp.y[(size_t)idx * qp.stride], qp.z[(size_t)idx * qp.stride]};
-  MinCand mc;
-  init_min(mc);
-  unsigned long long st[4];
-  if(!mixed_traverse<NPC, false>(q, mc, nodes64, nodes32, leaves64, leaves32, mesh_max, prm.sign != 0, st))
-    atomicOr(err, DEVERR_STACK);
-  const double sgn = query_sign<NPC>(q, mc, leaves64, prm);
+  const double sgn = signbit(dist[idx]) ? -1.0 : 1.0;
+  const int lc = leaf_code[idx];
   double u[3] = {0.0, 0.0, 0.0}, bary[3] = {0.0, 0.0, 0.0};
   int vid[3] = {0, 0, 0};
-  if(mc.leaf >= 0)
+  if(lc >= 0)
   {
+    const int leaf = lc >> 1, sub = lc & 1;
     double v[3 * NPC];
-    load_leaf<NPC>(leaves64, mc.leaf, v);
-    const int s1 = (NPC == 4 && mc.sub == 1) ? 2 : 1;
+    load_leaf<NPC>(leaves64, leaf, v);
+    const int s1 = (NPC == 4 && sub == 1) ? 2 : 1;
     const double* A = v;
     const double* B = v + 3 * s1;
     const double* C = v + 3 * (s1 + 1);
@@ -167,7 +133,7 @@ __global__ void __launch_bounds__(128) k_sdf_adjoint(const NodeRec64* __restrict
     const double r0 = q[0] - cp[0], r1 = q[1] - cp[1], r2 = q[2] - cp[2];
     const double len = sqrt(r0 * r0 + r1 * r1 + r2 * r2);
     if(len > 0.0) u[0] = r0 / len, u[1] = r1 / len, u[2] = r2 / len;
-    const int cell = __ldg(&leaves64[mc.leaf].cell);
+    const int cell = __ldg(&leaves64[leaf].cell);
     vid[0] = __ldg(cells + (size_t)cell * NPC);
     vid[1] = __ldg(cells + (size_t)cell * NPC + s1);
     vid[2] = __ldg(cells + (size_t)cell * NPC + s1 + 1);
@@ -278,18 +244,37 @@ int gsq_sdf_backward(const gsq_sdf* hc, const double* qx, const double* qy, cons
   std::memcpy(prm.domain, h->domain, sizeof(prm.domain));
   prm.watertight = h->watertight;
   prm.sign = h->sign;
+  // each point's signed distance and closest triangle from the persistent
+  // mixed query; its work counter is the handle's unless another thread holds
+  // it (held until the stream has synchronised below)
+  Scratch fwd;
+  GSQ_CUDA_TRY(fwd.alloc(align256(sizeof(double) * (size_t)m) + sizeof(int) * ((size_t)m + 64), s));
+  double* dist = fwd.as<double>();
+  int* leaf_code = reinterpret_cast<int*>(fwd.as<char>() + align256(sizeof(double) * (size_t)m));
+  int* work = leaf_code + m;
+  std::unique_lock<std::mutex> lock(h->work_busy, std::try_to_lock);
+  if(lock.owns_lock()) work = h->d_work;
+  GSQ_CUDA_TRY(cudaMemsetAsync(work, 0, sizeof(int), s));
   const int threads = 128;
-  count_launch();
+  cudaError_t e;
   if(h->npc == 3)
-    k_sdf_adjoint<3><<<grid_for(m, threads), threads, 0, s>>>(
-      B->nodes, h->nodes32, static_cast<const LeafRec<3>*>(h->leaves), static_cast<const LeafRec32<3>*>(h->leaves32),
-      h->d_cells, qp, m, order, prm, h->mesh_max, static_cast<const double*>(gb.dev), static_cast<double*>(gq.dev),
-      vkeys[0], contrib, h->d_err);
+    e = launch_mixed<3, false, 4, STACK_SIZE, false, true>(threads, s, B->nodes, h->nodes32, h->leaves, h->leaves32,
+                                                            h->d_mesh, 1, nullptr, qp, m, order, prm, dist, nullptr,
+                                                            nullptr, h->d_err, MixedStats {nullptr}, work, leaf_code);
   else
-    k_sdf_adjoint<4><<<grid_for(m, threads), threads, 0, s>>>(
-      B->nodes, h->nodes32, static_cast<const LeafRec<4>*>(h->leaves), static_cast<const LeafRec32<4>*>(h->leaves32),
-      h->d_cells, qp, m, order, prm, h->mesh_max, static_cast<const double*>(gb.dev), static_cast<double*>(gq.dev),
-      vkeys[0], contrib, h->d_err);
+    e = launch_mixed<4, false, 4, STACK_SIZE, false, true>(threads, s, B->nodes, h->nodes32, h->leaves, h->leaves32,
+                                                            h->d_mesh, 1, nullptr, qp, m, order, prm, dist, nullptr,
+                                                            nullptr, h->d_err, MixedStats {nullptr}, work, leaf_code);
+  GSQ_CUDA_TRY(e);
+  count_launch(2);
+  if(h->npc == 3)
+    k_adjoint_apply<3><<<grid_for(m, 256), 256, 0, s>>>(static_cast<const LeafRec<3>*>(h->leaves), h->d_cells, qp, m,
+                                                        dist, leaf_code, static_cast<const double*>(gb.dev),
+                                                        static_cast<double*>(gq.dev), vkeys[0], contrib);
+  else
+    k_adjoint_apply<4><<<grid_for(m, 256), 256, 0, s>>>(static_cast<const LeafRec<4>*>(h->leaves), h->d_cells, qp, m,
+                                                        dist, leaf_code, static_cast<const double*>(gb.dev),
+                                                        static_cast<double*>(gq.dev), vkeys[0], contrib);
   GSQ_CUDA_TRY(cudaGetLastError());
   if(nrec)
   {

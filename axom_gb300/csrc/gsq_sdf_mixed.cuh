@@ -260,49 +260,5 @@ __device__ __forceinline__ void leaf_refine(const LeafRec<NPC>* __restrict__ lea
   }
 }
 
-// The certified traversal for one point, one thread at a time (used by the
-// adjoint).  mc must be initialised.  Returns false on stack overflow.  With
-// AUDIT, stats[0..3] accumulate contradictions, FP64 node decisions, FP64
-// leaf checks and skips.
-template <int NPC, bool AUDIT>
-__device__ __forceinline__ bool mixed_traverse(const double* q, MinCand& mc, const NodeRec64* __restrict__ nodes64,
-                                               const NodeRec32* __restrict__ nodes32,
-                                               const LeafRec<NPC>* __restrict__ leaves64,
-                                               const LeafRec32<NPC>* __restrict__ leaves32, float mesh_max,
-                                               bool computeNormal, unsigned long long* stats)
-{
-  QCtx c;
-  qctx_init(c, q, mesh_max);
-  qctx_update(c, mc.minSq);
-  auto visit = [&](int cur, bool& inL, bool& inR, bool& swap, int2& ch) {
-    if(visit32(nodes32, cur, c, inL, inR, swap, ch))
-    {
-      if(AUDIT)
-      {
-        bool a2, b2, w2;
-        visit_fp64<false>(nodes64, cur, q, mc.minSq, a2, b2, w2);
-        if(a2 != inL || b2 != inR || (inL && inR && w2 != swap)) ++stats[0];
-      }
-      return;
-    }
-    if(AUDIT) ++stats[1];
-    visit_fp64<false>(nodes64, cur, q, mc.minSq, inL, inR, swap);
-  };
-  auto leaf = [&](int leafpos) {
-    const int need = leaf_prefilter<NPC>(leaves32, leafpos, c);
-    const int all = (1 << (NPC - 2)) - 1;
-    if(AUDIT)
-    {
-      if(need == 0) ++stats[3];
-      stats[0] += leaf_audit<NPC>(leaves64, leafpos, all & ~need, q, mc.minSq);
-    }
-    if(need == 0) return;
-    if(AUDIT) ++stats[2];
-    const double before = mc.minSq;
-    leaf_refine<NPC>(leaves64, leafpos, need, q, mc, computeNormal);
-    if(mc.minSq != before) qctx_update(c, mc.minSq);
-  };
-  return traverse_point(visit, leaf);
-}
 }  // namespace sdf
 }  // namespace gsq

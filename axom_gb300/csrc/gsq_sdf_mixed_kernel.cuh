@@ -46,8 +46,12 @@ struct MixedStats
 // constant measured: about 12 for uniform points, 24 near the surface).
 constexpr float BATCH_K = 38.5f, BATCH_LAM0 = 0.1f;
 constexpr int BATCH_LO = 8, BATCH_HI = 24;
+//
+// LEAF: also write each point's closest triangle (leaf position * 2 + the
+// triangle within the leaf; -1 when there is none) to out_leaf, for the
+// adjoint.
 
-template <int NPC, bool AUDIT, int QCAP, int STK, bool MULTI>
+template <int NPC, bool AUDIT, int QCAP, int STK, bool MULTI, bool LEAF = false>
 __global__ void __launch_bounds__(128, 5) k_sdf_mixed(const NodeRec64* __restrict__ nodes64_all,
                                                    const NodeRec32* __restrict__ nodes32_all,
                                                    const LeafRec<NPC>* __restrict__ leaves64_all,
@@ -64,7 +68,8 @@ __global__ void __launch_bounds__(128, 5) k_sdf_mixed(const NodeRec64* __restric
                                                    double* __restrict__ out_n,
                                                    int* err,
                                                    MixedStats stats,
-                                                   int* __restrict__ work)
+                                                   int* __restrict__ work,
+                                                   int* __restrict__ out_leaf)
 {
   constexpr unsigned FULL = 0xFFFFFFFFu;
   constexpr int M_DESCEND = 0, M_LEAF = 1, M_IDLE = 2;
@@ -282,6 +287,7 @@ __global__ void __launch_bounds__(128, 5) k_sdf_mixed(const NodeRec64* __restric
         }
         else
           finish_query<NPC>(q, mc, leaves64, prm_all, idx, out, out_cp, out_n, hint);
+        if constexpr(LEAF) out_leaf[idx] = (mc.leaf < 0) ? -1 : 2 * mc.leaf + mc.sub;
         mode = M_IDLE;
       }
       continue;
@@ -436,19 +442,20 @@ cudaError_t mixed_grid(K kernel, int threads, long long m, int* grid)
   return e;
 }
 
-template <int NPC, bool AUDIT, int QCAP, int STK, bool MULTI>
+template <int NPC, bool AUDIT, int QCAP, int STK, bool MULTI, bool LEAF = false>
 cudaError_t launch_mixed(int threads, cudaStream_t s, const NodeRec64* nodes64, const NodeRec32* nodes32,
                          const void* leaves64, const void* leaves32, const MeshInfo* meshes, int nmeshes,
                          const long long* qoff, const QueryPts& qp, int m, const int* order, const SdfParams& prm,
-                         double* out, double* out_cp, double* out_n, int* err, MixedStats st, int* work)
+                         double* out, double* out_cp, double* out_n, int* err, MixedStats st, int* work,
+                         int* out_leaf = nullptr)
 {
-  auto kernel = k_sdf_mixed<NPC, AUDIT, QCAP, STK, MULTI>;
+  auto kernel = k_sdf_mixed<NPC, AUDIT, QCAP, STK, MULTI, LEAF>;
   int g = 1;
   cudaError_t e = mixed_grid(kernel, threads, m, &g);
   if(e != cudaSuccess) return e;
   kernel<<<g, threads, 0, s>>>(nodes64, nodes32, static_cast<const LeafRec<NPC>*>(leaves64),
                                static_cast<const LeafRec32<NPC>*>(leaves32), meshes, nmeshes, qoff, qp, m, order, prm,
-                               out, out_cp, out_n, err, st, work);
+                               out, out_cp, out_n, err, st, work, out_leaf);
   return cudaGetLastError();
 }
 }  // namespace
