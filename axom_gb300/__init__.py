@@ -106,6 +106,8 @@ SIGNATURES = [
     ("gsq_sdf_last_eval_ms", C.c_int, [_vp, C.POINTER(C.c_float)]),
     ("gsq_sdf_mixed_stats", C.c_int, [_vp, _i64p]),
     ("gsq_sdf_backward", C.c_int, [_vp, _vp, _vp, _vp, C.c_int32, C.c_int32, _vp, _vp, _vp, _vp]),
+    ("gsq_sdf_eval_tri", C.c_int, [_vp, _vp, _vp, _vp, C.c_int32, C.c_int32, _vp, _vp, _vp]),
+    ("gsq_sdf_backward_tri", C.c_int, [_vp, _vp, _vp, _vp, C.c_int32, C.c_int32, _vp, _vp, _vp, _vp, _vp, _vp]),
     ("gsq_sdf_eval_noalloc", C.c_int, [_vp, _vp, _vp, _vp, C.c_int32, C.c_int32, _vp, _vp]),
     ("gsq_stl_read", C.c_int, [C.c_char_p, C.POINTER(_dp), _ip, C.POINTER(_ip), _ip]),
     ("gsq_bvh_get_view", C.c_int, [_vp, C.POINTER(BvhView)]),
@@ -437,17 +439,40 @@ class SignedDistance:
                                       xs.n, C.c_void_p(_ptr(out)), None, None, _stream()))
         return out
 
-    def backward(self, points, grad_dist, want_points: bool = True, want_vertices: bool = True):
-        """Adjoint of compute_distances: (dL/dpoints (m,3), dL/dvertices (V,3))."""
+    def compute_distances_tri(self, points, out=None):
+        """Signed distances of (m, 3) points and each point's closest triangle
+        (int32: c, or 2c / 2c + 1 within quad cell c; -1 for none), as a
+        forward pass saves them for backward(..., dist=, triangles=)."""
+        p = _Arr(points, np.float64, 3)
+        m = p.n
+        out = p.empty(m, np.float64) if out is None else out
+        tri = p.empty(m, np.int32)
+        base = p.ptr
+        _check(self._lib.gsq_sdf_eval_tri(self._h, C.c_void_p(base), C.c_void_p(base + 8), C.c_void_p(base + 16), 3,
+                                          m, C.c_void_p(_ptr(out)), C.c_void_p(_ptr(tri)), _stream()))
+        return out, tri
+
+    def backward(self, points, grad_dist, want_points: bool = True, want_vertices: bool = True, dist=None,
+                 triangles=None):
+        """Adjoint of compute_distances: (dL/dpoints (m,3), dL/dvertices (V,3)).
+        With the forward's dist and triangles (compute_distances_tri) the
+        closest triangles are not searched again."""
         p = _Arr(points, np.float64, 3)
         g = _Arr(grad_dist, np.float64)
         m = p.n
         gp = p.empty((m, 3), np.float64) if want_points else None
         gv = p.empty((self.num_vertices, 3), np.float64) if want_vertices else None
         base = p.ptr
-        _check(self._lib.gsq_sdf_backward(self._h, C.c_void_p(base), C.c_void_p(base + 8), C.c_void_p(base + 16), 3,
-                                          m, C.c_void_p(g.ptr), C.c_void_p(_ptr(gp)) if gp is not None else None,
-                                          C.c_void_p(_ptr(gv)) if gv is not None else None, _stream()))
+        outs = (C.c_void_p(_ptr(gp)) if gp is not None else None, C.c_void_p(_ptr(gv)) if gv is not None else None)
+        if triangles is not None:
+            d = _Arr(dist, np.float64)
+            t = _Arr(triangles, np.int32)
+            _check(self._lib.gsq_sdf_backward_tri(self._h, C.c_void_p(base), C.c_void_p(base + 8),
+                                                  C.c_void_p(base + 16), 3, m, C.c_void_p(d.ptr), C.c_void_p(t.ptr),
+                                                  C.c_void_p(g.ptr), *outs, _stream()))
+        else:
+            _check(self._lib.gsq_sdf_backward(self._h, C.c_void_p(base), C.c_void_p(base + 8), C.c_void_p(base + 16),
+                                              3, m, C.c_void_p(g.ptr), *outs, _stream()))
         return gp, gv
 
     def compute_distance(self, x: float, y: float, z: float) -> float:

@@ -49,6 +49,7 @@ __global__ void __launch_bounds__(128) k_sdf_fp64(const NodeRec64* __restrict__ 
                                                   double* __restrict__ out,
                                                   double* __restrict__ out_cp,
                                                   double* __restrict__ out_n,
+                                                  int* __restrict__ out_tri,
                                                   int* err)
 {
   const int t = blockIdx.x * blockDim.x + threadIdx.x;
@@ -65,6 +66,12 @@ __global__ void __launch_bounds__(128) k_sdf_fp64(const NodeRec64* __restrict__ 
   auto leaf = [&](int leafpos) { check_leaf<NPC>(q, mc, leaves, leafpos, computeNormal); };
   if(!traverse_point(visit, leaf)) atomicOr(err, DEVERR_STACK);
   finish_query<NPC>(q, mc, leaves, prm, idx, out, out_cp, out_n);
+  if(out_tri)
+  {
+    // the closest triangle (c, or 2c / 2c + 1 within quad cell c; -1: none)
+    const int cell = (mc.leaf < 0) ? -1 : __ldg(&leaves[mc.leaf].cell);
+    out_tri[idx] = (cell < 0) ? -1 : (NPC == 3 ? cell : 2 * cell + mc.sub);
+  }
 }
 
 // Per-cell bounding boxes (getCellBoundingBox, SD:608-633): addPoint of each
@@ -424,8 +431,14 @@ int gsq_sdf_last_eval_ms(const gsq_sdf* h, float* ms)
   return GSQ_OK;
 }
 
-int gsq_sdf_eval(const gsq_sdf* hc, const double* qx, const double* qy, const double* qz, int32_t stride, int32_t m,
-                 double* out, double* closest, double* normals, void* stream)
+}  // extern "C"
+
+namespace
+{
+// gsq_sdf_eval and gsq_sdf_eval_tri: tri (nullable) receives each point's
+// closest triangle.
+int sdf_eval_impl(const gsq_sdf* hc, const double* qx, const double* qy, const double* qz, int32_t stride, int32_t m,
+                  double* out, double* closest, double* normals, int32_t* tri, void* stream)
 {
   gsq_sdf* h = const_cast<gsq_sdf*>(hc);
   if(!h) return fail(GSQ_ERR_INVALID, "null sdf handle");
@@ -441,15 +454,16 @@ int gsq_sdf_eval(const gsq_sdf* hc, const double* qx, const double* qy, const do
   const bool cached = lock.owns_lock();
   const bool sort = h->opts.sort_queries && m > 1;
   const size_t in_bytes = stage_query_bytes(qx, qy, qz, stride, m);
-  const size_t out_bytes[3] = {is_device_ptr(out) ? 0 : align256(sizeof(double) * (size_t)m),
+  const size_t out_bytes[4] = {is_device_ptr(out) ? 0 : align256(sizeof(double) * (size_t)m),
                                (!closest || is_device_ptr(closest)) ? 0 : align256(sizeof(double) * 3 * (size_t)m),
-                               (!normals || is_device_ptr(normals)) ? 0 : align256(sizeof(double) * 3 * (size_t)m)};
+                               (!normals || is_device_ptr(normals)) ? 0 : align256(sizeof(double) * 3 * (size_t)m),
+                               (!tri || is_device_ptr(tri)) ? 0 : align256(sizeof(int32_t) * (size_t)m)};
   const size_t order_bytes = sort ? align256(4 * sizeof(uint32_t) * (size_t)m) : 0;
   const size_t sort_bytes = sort ? align256(radix_sort_work_bytes(m)) : 0;
   char* cv = nullptr;
   if(cached)
   {
-    const size_t need = in_bytes + out_bytes[0] + out_bytes[1] + out_bytes[2] + order_bytes + sort_bytes;
+    const size_t need = in_bytes + out_bytes[0] + out_bytes[1] + out_bytes[2] + out_bytes[3] + order_bytes + sort_bytes;
     if(need > h->eval_bytes)
     {
       if(h->eval_buf) cudaFree(h->eval_buf);
@@ -470,10 +484,11 @@ int gsq_sdf_eval(const gsq_sdf* hc, const double* qx, const double* qy, const do
   QueryPts qp;
   int rc = stage_queries(qx, qy, qz, stride, m, s, qb, qp, take(in_bytes));
   if(rc) return rc;
-  OutBuf ob, cb, nb;
+  OutBuf ob, cb, nb, tb;
   GSQ_CUDA_TRY(ob.prepare(out, sizeof(double) * (size_t)m, s, take(out_bytes[0])));
   GSQ_CUDA_TRY(cb.prepare(closest, sizeof(double) * 3 * (size_t)m, s, take(out_bytes[1])));
   GSQ_CUDA_TRY(nb.prepare(normals, sizeof(double) * 3 * (size_t)m, s, take(out_bytes[2])));
+  GSQ_CUDA_TRY(tb.prepare(tri, sizeof(int32_t) * (size_t)m, s, take(out_bytes[3])));
 
   const BvhDev* B = bvh_dev(h->bvh);
   Scratch order_buf;
@@ -525,9 +540,14 @@ int gsq_sdf_eval(const gsq_sdf* hc, const double* qx, const double* qy, const do
       GSQ_CUDA_TRY(own_work.alloc(sizeof(int), s));
       work = own_work.as<int>();
     }
-    rc = mixed_launch(h->npc, B->nodes, h->nodes32, h->leaves, h->leaves32, h->d_mesh, qp, m, order, prm,
-                      static_cast<double*>(ob.dev), static_cast<double*>(cb.dev), static_cast<double*>(nb.dev),
-                      h->d_err, audit ? h->d_audit : nullptr, work, h->opts.block_size, h->opts.queue_depth, s);
+    if(tri)
+      rc = mixed_launch_tri(h->npc, B->nodes, h->nodes32, h->leaves, h->leaves32, h->d_mesh, qp, m, order, prm,
+                            static_cast<double*>(ob.dev), static_cast<double*>(cb.dev), static_cast<double*>(nb.dev),
+                            h->d_err, work, static_cast<int*>(tb.dev), s);
+    else
+      rc = mixed_launch(h->npc, B->nodes, h->nodes32, h->leaves, h->leaves32, h->d_mesh, qp, m, order, prm,
+                        static_cast<double*>(ob.dev), static_cast<double*>(cb.dev), static_cast<double*>(nb.dev),
+                        h->d_err, audit ? h->d_audit : nullptr, work, h->opts.block_size, h->opts.queue_depth, s);
     if(rc) return rc;
   }
   else
@@ -536,12 +556,12 @@ int gsq_sdf_eval(const gsq_sdf* hc, const double* qx, const double* qy, const do
     k_sdf_fp64<3><<<grid_for(m, threads), threads, 0, s>>>(B->nodes, static_cast<const LeafRec<3>*>(h->leaves), qp, m,
                                                           order, prm, static_cast<double*>(ob.dev),
                                                           static_cast<double*>(cb.dev), static_cast<double*>(nb.dev),
-                                                          h->d_err);
+                                                          static_cast<int*>(tb.dev), h->d_err);
   else if(!mixed)
     k_sdf_fp64<4><<<grid_for(m, threads), threads, 0, s>>>(B->nodes, static_cast<const LeafRec<4>*>(h->leaves), qp, m,
                                                           order, prm, static_cast<double*>(ob.dev),
                                                           static_cast<double*>(cb.dev), static_cast<double*>(nb.dev),
-                                                          h->d_err);
+                                                          static_cast<int*>(tb.dev), h->d_err);
   cudaEventRecord(e1, s);
   cudaError_t e = cudaGetLastError();
   if(audit && e == cudaSuccess)
@@ -549,12 +569,29 @@ int gsq_sdf_eval(const gsq_sdf* hc, const double* qx, const double* qy, const do
   if(e == cudaSuccess) e = ob.flush(s);
   if(e == cudaSuccess) e = cb.flush(s);
   if(e == cudaSuccess) e = nb.flush(s);
+  if(e == cudaSuccess) e = tb.flush(s);
   if(e == cudaSuccess) e = cudaStreamSynchronize(s);
   cudaEventElapsedTime(&h->eval_ms, e0, e1);
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
   if(e != cudaSuccess) return cuda_fail(e, "gsq_sdf_eval");
   return check_device_error(h->d_err, s, "gsq_sdf_eval");
+}
+}  // namespace
+
+extern "C" {
+
+int gsq_sdf_eval(const gsq_sdf* h, const double* qx, const double* qy, const double* qz, int32_t stride, int32_t m,
+                 double* out, double* closest, double* normals, void* stream)
+{
+  return sdf_eval_impl(h, qx, qy, qz, stride, m, out, closest, normals, nullptr, stream);
+}
+
+int gsq_sdf_eval_tri(const gsq_sdf* h, const double* qx, const double* qy, const double* qz, int32_t stride,
+                     int32_t m, double* out, int32_t* triangles, void* stream)
+{
+  if(m > 0 && !triangles) return fail(GSQ_ERR_INVALID, "null triangle array");
+  return sdf_eval_impl(h, qx, qy, qz, stride, m, out, nullptr, nullptr, triangles, stream);
 }
 
 }  // extern "C"
@@ -676,10 +713,10 @@ int gsq_sdf_eval_noalloc(const gsq_sdf* hc, const double* qx, const double* qy, 
     count_launch();
     if(h->npc == 3)
       k_sdf_fp64<3><<<grid_for(m, threads), threads, 0, s>>>(B->nodes, static_cast<const LeafRec<3>*>(h->leaves), qp,
-                                                            m, order, prm, out, nullptr, nullptr, h->d_err);
+                                                            m, order, prm, out, nullptr, nullptr, nullptr, h->d_err);
     else
       k_sdf_fp64<4><<<grid_for(m, threads), threads, 0, s>>>(B->nodes, static_cast<const LeafRec<4>*>(h->leaves), qp,
-                                                            m, order, prm, out, nullptr, nullptr, h->d_err);
+                                                            m, order, prm, out, nullptr, nullptr, nullptr, h->d_err);
   }
   GSQ_CUDA_TRY(cudaGetLastError());
   return check_device_error(h->d_err, s, "gsq_sdf_eval_noalloc");

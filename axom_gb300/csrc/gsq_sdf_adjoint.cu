@@ -97,16 +97,17 @@ __device__ __forceinline__ void closest_point_bary(const double* P, const double
   bary[0] = 1.0 - v - w, bary[1] = v, bary[2] = w;
 }
 
-// Per point: the gradient directions from its closest triangle (leaf code
-// from the mixed query: leaf position * 2 + triangle, -1 for none) and the
-// sign of its signed distance d = sqrt(minSq) * sign.
+// Per point: the gradient directions from its closest triangle (tri: c, or
+// 2c / 2c + 1 within quad cell c; -1 for none), whose vertices are read from
+// the mesh arrays (the values the leaf records hold), and the sign of its
+// signed distance d = sqrt(minSq) * sign.
 template <int NPC>
-__global__ void __launch_bounds__(256) k_adjoint_apply(const LeafRec<NPC>* __restrict__ leaves64,
-                                                       const int* __restrict__ cells,
+__global__ void __launch_bounds__(256) k_adjoint_apply(const double* __restrict__ x, const double* __restrict__ y,
+                                                       const double* __restrict__ z, const int* __restrict__ cells,
                                                        QueryPts qp,
                                                        int m,
                                                        const double* __restrict__ dist,
-                                                       const int* __restrict__ leaf_code,
+                                                       const int* __restrict__ tri,
                                                        const double* __restrict__ grad_d,
                                                        double* __restrict__ grad_q,
                                                        uint32_t* __restrict__ vkeys,
@@ -116,27 +117,28 @@ __global__ void __launch_bounds__(256) k_adjoint_apply(const LeafRec<NPC>* __res
   if(idx >= m) return;
   const double q[3] = {qp.x[(size_t)idx * qp.stride], qp.y[(size_t)idx * qp.stride], qp.z[(size_t)idx * qp.stride]};
   const double sgn = signbit(dist[idx]) ? -1.0 : 1.0;
-  const int lc = leaf_code[idx];
+  const int t = tri[idx];
   double u[3] = {0.0, 0.0, 0.0}, bary[3] = {0.0, 0.0, 0.0};
   int vid[3] = {0, 0, 0};
-  if(lc >= 0)
+  if(t >= 0)
   {
-    const int leaf = lc >> 1, sub = lc & 1;
-    double v[3 * NPC];
-    load_leaf<NPC>(leaves64, leaf, v);
-    const int s1 = (NPC == 4 && sub == 1) ? 2 : 1;
-    const double* A = v;
-    const double* B = v + 3 * s1;
-    const double* C = v + 3 * (s1 + 1);
-    double cp[3];
-    closest_point_bary(q, A, B, C, cp, bary);
-    const double r0 = q[0] - cp[0], r1 = q[1] - cp[1], r2 = q[2] - cp[2];
-    const double len = sqrt(r0 * r0 + r1 * r1 + r2 * r2);
-    if(len > 0.0) u[0] = r0 / len, u[1] = r1 / len, u[2] = r2 / len;
-    const int cell = __ldg(&leaves64[leaf].cell);
+    const int cell = (NPC == 3) ? t : (t >> 1);
+    const int s1 = (NPC == 4 && (t & 1)) ? 2 : 1;
     vid[0] = __ldg(cells + (size_t)cell * NPC);
     vid[1] = __ldg(cells + (size_t)cell * NPC + s1);
     vid[2] = __ldg(cells + (size_t)cell * NPC + s1 + 1);
+    double v[9];
+    for(int k = 0; k < 3; ++k)
+    {
+      v[3 * k] = __ldg(x + vid[k]);
+      v[3 * k + 1] = __ldg(y + vid[k]);
+      v[3 * k + 2] = __ldg(z + vid[k]);
+    }
+    double cp[3];
+    closest_point_bary(q, v, v + 3, v + 6, cp, bary);
+    const double r0 = q[0] - cp[0], r1 = q[1] - cp[1], r2 = q[2] - cp[2];
+    const double len = sqrt(r0 * r0 + r1 * r1 + r2 * r2);
+    if(len > 0.0) u[0] = r0 / len, u[1] = r1 / len, u[2] = r2 / len;
   }
   const double coef = grad_d[idx] * sgn;
   if(grad_q)
@@ -186,12 +188,38 @@ int vertex_key_bits(int nverts)
 }  // namespace
 }  // namespace gsq
 
+namespace gsq
+{
+int mixed_launch_tri(int npc, const NodeRec64* nodes64, const NodeRec32* nodes32, const void* leaves64,
+                     const void* leaves32, const MeshInfo* meshes, const sdf::QueryPts& qp, int m, const int* order,
+                     const sdf::SdfParams& prm, double* out, double* out_cp, double* out_n, int* err, int* work,
+                     int* tri, cudaStream_t s)
+{
+  GSQ_CUDA_TRY(cudaMemsetAsync(work, 0, sizeof(int), s));
+  cudaError_t e;
+  if(npc == 3)
+    e = launch_mixed<3, false, 4, STACK_SIZE, false, true>(128, s, nodes64, nodes32, leaves64, leaves32, meshes, 1,
+                                                            nullptr, qp, m, order, prm, out, out_cp, out_n, err,
+                                                            MixedStats {nullptr}, work, tri);
+  else
+    e = launch_mixed<4, false, 4, STACK_SIZE, false, true>(128, s, nodes64, nodes32, leaves64, leaves32, meshes, 1,
+                                                            nullptr, qp, m, order, prm, out, out_cp, out_n, err,
+                                                            MixedStats {nullptr}, work, tri);
+  count_launch();
+  GSQ_CUDA_TRY(e);
+  return GSQ_OK;
+}
+}  // namespace gsq
+
 using namespace gsq;
 
-extern "C" {
-
-int gsq_sdf_backward(const gsq_sdf* hc, const double* qx, const double* qy, const double* qz, int32_t stride,
-                     int32_t m, const double* grad_dist, double* grad_points, double* grad_vertices, void* stream)
+namespace
+{
+// gsq_sdf_backward and gsq_sdf_backward_tri: with dist_in and tri_in null,
+// the closest triangles come from the mixed query run here.
+int backward_impl(const gsq_sdf* hc, const double* qx, const double* qy, const double* qz, int32_t stride, int32_t m,
+                  const double* dist_in, const int32_t* tri_in, const double* grad_dist, double* grad_points,
+                  double* grad_vertices, void* stream)
 {
   gsq_sdf* h = const_cast<gsq_sdf*>(hc);
   if(!h) return fail(GSQ_ERR_INVALID, "null sdf handle");
@@ -208,22 +236,51 @@ int gsq_sdf_backward(const gsq_sdf* hc, const double* qx, const double* qy, cons
     GSQ_CUDA_TRY(cudaStreamSynchronize(s));
     return GSQ_OK;
   }
-  InBuf qb[3], gb;
+  InBuf qb[3], gb, db, tb;
   sdf::QueryPts qp;
   int rc = stage_query_points(qx, qy, qz, stride, m, s, qb, qp);
   if(rc) return rc;
   GSQ_CUDA_TRY(gb.stage(grad_dist, sizeof(double) * (size_t)m, s));
   GSQ_CUDA_TRY(gq.prepare(grad_points, sizeof(double) * 3 * (size_t)m, s));
 
-  const BvhDev* B = bvh_dev(h->bvh);
-  Scratch order_buf;
-  GSQ_CUDA_TRY(order_buf.alloc(4 * sizeof(uint32_t) * (size_t)m, s));
-  uint32_t* okeys[2] = {order_buf.as<uint32_t>(), order_buf.as<uint32_t>() + m};
-  int* ovals[2] = {reinterpret_cast<int*>(order_buf.as<uint32_t>() + 2 * (size_t)m),
-                   reinterpret_cast<int*>(order_buf.as<uint32_t>() + 3 * (size_t)m)};
-  const int* order = nullptr;
-  rc = sdf_query_order(h, qp, m, okeys, ovals, &order, s);
-  if(rc) return rc;
+  const double* dist = nullptr;
+  const int* tri = nullptr;
+  Scratch order_buf, fwd;
+  // the work counter of the mixed query: the handle's unless another thread
+  // holds it (held until the stream has synchronised below)
+  std::unique_lock<std::mutex> lock(h->work_busy, std::defer_lock);
+  if(tri_in)
+  {
+    GSQ_CUDA_TRY(db.stage(dist_in, sizeof(double) * (size_t)m, s));
+    GSQ_CUDA_TRY(tb.stage(tri_in, sizeof(int32_t) * (size_t)m, s));
+    dist = static_cast<const double*>(db.dev);
+    tri = static_cast<const int*>(tb.dev);
+  }
+  else
+  {
+    const BvhDev* B = bvh_dev(h->bvh);
+    GSQ_CUDA_TRY(order_buf.alloc(4 * sizeof(uint32_t) * (size_t)m, s));
+    uint32_t* okeys[2] = {order_buf.as<uint32_t>(), order_buf.as<uint32_t>() + m};
+    int* ovals[2] = {reinterpret_cast<int*>(order_buf.as<uint32_t>() + 2 * (size_t)m),
+                     reinterpret_cast<int*>(order_buf.as<uint32_t>() + 3 * (size_t)m)};
+    const int* order = nullptr;
+    rc = sdf_query_order(h, qp, m, okeys, ovals, &order, s);
+    if(rc) return rc;
+    GSQ_CUDA_TRY(fwd.alloc(align256(sizeof(double) * (size_t)m) + sizeof(int) * ((size_t)m + 64), s));
+    double* d = fwd.as<double>();
+    int* t = reinterpret_cast<int*>(fwd.as<char>() + align256(sizeof(double) * (size_t)m));
+    int* work = t + m;
+    if(lock.try_lock()) work = h->d_work;
+    sdf::SdfParams prm;
+    std::memcpy(prm.domain, h->domain, sizeof(prm.domain));
+    prm.watertight = h->watertight;
+    prm.sign = h->sign;
+    rc = mixed_launch_tri(h->npc, B->nodes, h->nodes32, h->leaves, h->leaves32, h->d_mesh, qp, m, order, prm, d,
+                          nullptr, nullptr, h->d_err, work, t, s);
+    if(rc) return rc;
+    dist = d;
+    tri = t;
+  }
 
   const long long nrec = gv.dev ? 3ll * m : 0;
   Scratch rec_buf;
@@ -240,40 +297,14 @@ int gsq_sdf_backward(const gsq_sdf* hc, const double* qx, const double* qy, cons
     vvals[0] = reinterpret_cast<int*>(w + 2 * nrec);
     vvals[1] = reinterpret_cast<int*>(w + 3 * nrec);
   }
-  sdf::SdfParams prm;
-  std::memcpy(prm.domain, h->domain, sizeof(prm.domain));
-  prm.watertight = h->watertight;
-  prm.sign = h->sign;
-  // each point's signed distance and closest triangle from the persistent
-  // mixed query; its work counter is the handle's unless another thread holds
-  // it (held until the stream has synchronised below)
-  Scratch fwd;
-  GSQ_CUDA_TRY(fwd.alloc(align256(sizeof(double) * (size_t)m) + sizeof(int) * ((size_t)m + 64), s));
-  double* dist = fwd.as<double>();
-  int* leaf_code = reinterpret_cast<int*>(fwd.as<char>() + align256(sizeof(double) * (size_t)m));
-  int* work = leaf_code + m;
-  std::unique_lock<std::mutex> lock(h->work_busy, std::try_to_lock);
-  if(lock.owns_lock()) work = h->d_work;
-  GSQ_CUDA_TRY(cudaMemsetAsync(work, 0, sizeof(int), s));
-  const int threads = 128;
-  cudaError_t e;
+  count_launch();
   if(h->npc == 3)
-    e = launch_mixed<3, false, 4, STACK_SIZE, false, true>(threads, s, B->nodes, h->nodes32, h->leaves, h->leaves32,
-                                                            h->d_mesh, 1, nullptr, qp, m, order, prm, dist, nullptr,
-                                                            nullptr, h->d_err, MixedStats {nullptr}, work, leaf_code);
-  else
-    e = launch_mixed<4, false, 4, STACK_SIZE, false, true>(threads, s, B->nodes, h->nodes32, h->leaves, h->leaves32,
-                                                            h->d_mesh, 1, nullptr, qp, m, order, prm, dist, nullptr,
-                                                            nullptr, h->d_err, MixedStats {nullptr}, work, leaf_code);
-  GSQ_CUDA_TRY(e);
-  count_launch(2);
-  if(h->npc == 3)
-    k_adjoint_apply<3><<<grid_for(m, 256), 256, 0, s>>>(static_cast<const LeafRec<3>*>(h->leaves), h->d_cells, qp, m,
-                                                        dist, leaf_code, static_cast<const double*>(gb.dev),
+    k_adjoint_apply<3><<<grid_for(m, 256), 256, 0, s>>>(h->d_x, h->d_y, h->d_z, h->d_cells, qp, m, dist, tri,
+                                                        static_cast<const double*>(gb.dev),
                                                         static_cast<double*>(gq.dev), vkeys[0], contrib);
   else
-    k_adjoint_apply<4><<<grid_for(m, 256), 256, 0, s>>>(static_cast<const LeafRec<4>*>(h->leaves), h->d_cells, qp, m,
-                                                        dist, leaf_code, static_cast<const double*>(gb.dev),
+    k_adjoint_apply<4><<<grid_for(m, 256), 256, 0, s>>>(h->d_x, h->d_y, h->d_z, h->d_cells, qp, m, dist, tri,
+                                                        static_cast<const double*>(gb.dev),
                                                         static_cast<double*>(gq.dev), vkeys[0], contrib);
   GSQ_CUDA_TRY(cudaGetLastError());
   if(nrec)
@@ -289,6 +320,23 @@ int gsq_sdf_backward(const gsq_sdf* hc, const double* qx, const double* qy, cons
   GSQ_CUDA_TRY(gv.flush(s));
   GSQ_CUDA_TRY(cudaStreamSynchronize(s));
   return check_device_error(h->d_err, s, "gsq_sdf_backward");
+}
+}  // namespace
+
+extern "C" {
+
+int gsq_sdf_backward(const gsq_sdf* h, const double* qx, const double* qy, const double* qz, int32_t stride,
+                     int32_t m, const double* grad_dist, double* grad_points, double* grad_vertices, void* stream)
+{
+  return backward_impl(h, qx, qy, qz, stride, m, nullptr, nullptr, grad_dist, grad_points, grad_vertices, stream);
+}
+
+int gsq_sdf_backward_tri(const gsq_sdf* h, const double* qx, const double* qy, const double* qz, int32_t stride,
+                         int32_t m, const double* dist, const int32_t* triangles, const double* grad_dist,
+                         double* grad_points, double* grad_vertices, void* stream)
+{
+  if(m > 0 && (!dist || !triangles)) return fail(GSQ_ERR_INVALID, "null distance or triangle array");
+  return backward_impl(h, qx, qy, qz, stride, m, dist, triangles, grad_dist, grad_points, grad_vertices, stream);
 }
 
 }  // extern "C"

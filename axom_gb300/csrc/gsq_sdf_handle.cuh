@@ -48,6 +48,12 @@ int mixed_launch(int npc, const NodeRec64* nodes64, const NodeRec32* nodes32, co
                  const void* leaves32, const MeshInfo* meshes, const sdf::QueryPts& qp, int m, const int* order,
                  const sdf::SdfParams& prm, double* out, double* out_cp, double* out_n, int* err,
                  unsigned long long* audit, int* work, int block, int depth, cudaStream_t s);
+// The same query (128 threads, queue depth 4, no audit) also writing each
+// point's closest triangle to tri (c, or 2c / 2c + 1 within quad cell c).
+int mixed_launch_tri(int npc, const NodeRec64* nodes64, const NodeRec32* nodes32, const void* leaves64,
+                     const void* leaves32, const MeshInfo* meshes, const sdf::QueryPts& qp, int m, const int* order,
+                     const sdf::SdfParams& prm, double* out, double* out_cp, double* out_n, int* err, int* work,
+                     int* tri, cudaStream_t s);
 }  // namespace gsq
 
 namespace gsq

@@ -47,9 +47,9 @@ struct MixedStats
 constexpr float BATCH_K = 38.5f, BATCH_LAM0 = 0.1f;
 constexpr int BATCH_LO = 8, BATCH_HI = 24;
 //
-// LEAF: also write each point's closest triangle (leaf position * 2 + the
-// triangle within the leaf; -1 when there is none) to out_leaf, for the
-// adjoint.
+// LEAF: also write each point's closest triangle to out_leaf: c for triangle
+// cell c, 2c or 2c + 1 for the first or second triangle of quad cell c, -1
+// when there is none (for the adjoint).
 
 template <int NPC, bool AUDIT, int QCAP, int STK, bool MULTI, bool LEAF = false>
 __global__ void __launch_bounds__(128, 5) k_sdf_mixed(const NodeRec64* __restrict__ nodes64_all,
@@ -287,7 +287,11 @@ __global__ void __launch_bounds__(128, 5) k_sdf_mixed(const NodeRec64* __restric
         }
         else
           finish_query<NPC>(q, mc, leaves64, prm_all, idx, out, out_cp, out_n, hint);
-        if constexpr(LEAF) out_leaf[idx] = (mc.leaf < 0) ? -1 : 2 * mc.leaf + mc.sub;
+        if constexpr(LEAF)
+        {
+          const int cell = (mc.leaf < 0) ? -1 : __ldg(&leaves64[mc.leaf].cell);
+          out_leaf[idx] = (cell < 0) ? -1 : (NPC == 3 ? cell : 2 * cell + mc.sub);
+        }
         mode = M_IDLE;
       }
       continue;

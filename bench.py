@@ -413,8 +413,9 @@ def near_surface_leg(args, G, torch, v, f):
 
 def adjoint_leg(args, G, torch):
     """Differentiated form: level-6 displaced icosphere (81,920 triangles),
-    1,048,576 uniform points, L = sum w d^2 with w ~ U[0,1]: forward (mixed)
-    plus the hand-written adjoint (dL/dpoints and the deterministic vertex
+    1,048,576 uniform points, L = sum w d^2 with w ~ U[0,1]: forward (mixed,
+    saving each point's closest triangle as an autograd forward would) plus
+    the hand-written adjoint (dL/dpoints and the deterministic vertex
     reduction) per step."""
     from axom_gb300 import workloads as W
     v, f = W.displaced_icosphere(6, MESH_SEED)
@@ -424,8 +425,8 @@ def adjoint_leg(args, G, torch):
     sd = G.SignedDistance(v, f, precision=G.PRECISION_MIXED)
 
     def step():
-        d = sd.compute_distances(q)
-        return sd.backward(q, 2.0 * w * d)
+        d, tri = sd.compute_distances_tri(q)
+        return sd.backward(q, 2.0 * w * d, dist=d, triangles=tri)
 
     for _ in range(args.warmup):
         step()
@@ -439,7 +440,7 @@ def adjoint_leg(args, G, torch):
     ms = ev0.elapsed_time(ev1) / args.steps
     gp2, gv2 = step()
     return {"workload": f"level-6 mesh ({f.shape[0]} triangles, {v.shape[0]} vertices), {m} uniform points, "
-                        "forward + backward per step",
+                        "forward (distances and closest triangles) + backward per step",
             "value": m / (ms / 1000.0), "unit": "points/s (forward + backward)", "ms_per_step": ms,
             "deterministic": bool(torch.equal(gv.view(torch.int64), gv2.view(torch.int64)))}
 

@@ -259,6 +259,24 @@ int gsq_sdf_last_eval_ms(const gsq_sdf* sdf, float* ms);
 int gsq_sdf_backward(const gsq_sdf* sdf, const double* qx, const double* qy, const double* qz, int32_t stride,
                      int32_t m, const double* grad_dist, double* grad_points, double* grad_vertices, void* stream);
 
+/* gsq_sdf_eval of the signed distances (no closest points or normals) that
+ * also returns each point's closest triangle, the one whose closest point the
+ * distance is measured to: triangles[i] = c for triangle cell c, 2c or 2c+1
+ * for the first (nodes 0, 1, 2) or second (nodes 0, 2, 3) triangle of quad
+ * cell c, -1 when the mesh has no valid cell.  In MIXED precision the query
+ * runs with 128 threads per block, queue depth 4 and no audit whatever the
+ * handle's options; distances equal gsq_sdf_eval's.  Saved by a forward pass
+ * for gsq_sdf_backward_tri.  No counterpart in the reference. */
+int gsq_sdf_eval_tri(const gsq_sdf* sdf, const double* qx, const double* qy, const double* qz, int32_t stride,
+                     int32_t m, double* out, int32_t* triangles, void* stream);
+
+/* gsq_sdf_backward given the forward pass's signed distances `dist` and
+ * closest triangles (gsq_sdf_eval_tri on the same points): the same outputs,
+ * bit for bit, without a second traversal. */
+int gsq_sdf_backward_tri(const gsq_sdf* sdf, const double* qx, const double* qy, const double* qz, int32_t stride,
+                         int32_t m, const double* dist, const int32_t* triangles, const double* grad_dist,
+                         double* grad_points, double* grad_vertices, void* stream);
+
 /* Counters of the last audited MIXED evaluation (opts.audit = 1), host int64[4]:
  *   [0] FP32 skips that the FP64 re-check contradicts (must be 0)
  *   [1] node visits decided in FP64   [2] leaves refined in FP64

@@ -186,3 +186,63 @@ def test_backward_is_deterministic(gsq, case):
     c = case["sd"].backward(case["qd"], g)
     case["sd"].set_sort_queries(True)
     assert torch.equal(a[1].view(torch.int64), c[1].view(torch.int64))
+
+
+def point_triangle_distance(p, a, b, c):
+    """Distance of points p (n, 3) to triangles (a, b, c) (n, 3 each), by the
+    projection onto the plane and the three edges (plain numpy, not the
+    reference's operation order)."""
+    def seg(p, a, b):
+        ab = b - a
+        t = np.clip(np.einsum("ij,ij->i", p - a, ab) / np.maximum(np.einsum("ij,ij->i", ab, ab), 1e-300), 0.0, 1.0)
+        return np.linalg.norm(p - (a + t[:, None] * ab), axis=1)
+    n = np.cross(b - a, c - a)
+    nn = np.linalg.norm(n, axis=1)
+    n = n / np.maximum(nn, 1e-300)[:, None]
+    h = np.einsum("ij,ij->i", p - a, n)
+    proj = p - h[:, None] * n
+    def inside(x, u, v, w):
+        return np.einsum("ij,ij->i", np.cross(v - u, x - u), n) >= 0
+    ins = inside(proj, a, b, c) & inside(proj, b, c, a) & inside(proj, c, a, b)
+    d = np.minimum(np.minimum(seg(p, a, b), seg(p, b, c)), seg(p, c, a))
+    return np.where(ins, np.abs(h), d)
+
+
+@pytest.mark.parametrize("precision", ["mixed", "fp64"])
+def test_eval_tri_distances_and_triangles(gsq, case, precision):
+    """gsq_sdf_eval_tri: the distances equal gsq_sdf_eval's bit for bit, and
+    each point's distance to its returned triangle is |d|."""
+    import torch
+    sd = case["sd"]
+    sd.set_precision(axom_gb300.PRECISION_MIXED if precision == "mixed" else axom_gb300.PRECISION_FP64)
+    try:
+        n = 1 << 16
+        qd = case["qd"][:n].contiguous()
+        d, tri = sd.compute_distances_tri(qd)
+        want = sd.compute_distances(qd)
+    finally:
+        sd.set_precision(axom_gb300.PRECISION_MIXED)
+    assert torch.equal(d.view(torch.int64), want.view(torch.int64))
+    t = tri.cpu().numpy()
+    assert (t >= 0).all() and (t < case["f"].shape[0]).all()
+    v, f = case["v"], case["f"][t]
+    dt = point_triangle_distance(case["q"][:n], v[f[:, 0]], v[f[:, 1]], v[f[:, 2]])
+    np.testing.assert_allclose(dt, np.abs(d.cpu().numpy()), rtol=1e-9, atol=1e-14)
+
+
+def test_backward_with_forward_triangles(gsq, case):
+    """gsq_sdf_backward_tri with the forward's distances and triangles gives
+    gsq_sdf_backward's outputs bit for bit, with device and host buffers."""
+    import torch
+    sd = case["sd"]
+    d, tri = sd.compute_distances_tri(case["qd"])
+    g = (2.0 * torch.from_numpy(case["w"]).cuda() * d).contiguous()
+    a = sd.backward(case["qd"], g)
+    b = sd.backward(case["qd"], g, dist=d, triangles=tri)
+    assert torch.equal(a[0].view(torch.int64), b[0].view(torch.int64))
+    assert torch.equal(a[1].view(torch.int64), b[1].view(torch.int64))
+    n = 1 << 14
+    h = sd.backward(case["q"][:n], g[:n].cpu().numpy(), dist=d[:n].cpu().numpy(), triangles=tri[:n].cpu().numpy())
+    r = sd.backward(case["qd"][:n].contiguous(), g[:n].contiguous())
+    assert np.array_equal(h[0].view(np.int64), r[0].cpu().numpy().view(np.int64))
+    assert np.array_equal(h[1].view(np.int64), r[1].cpu().numpy().view(np.int64))
