@@ -81,7 +81,7 @@ def test_config1_full_size_matches_oracle(gsq, port, scale):
     assert want[2].size > 4000
 
 
-@pytest.mark.parametrize("n", [0, 1, 2, 3, 5, 17, 100, 4095, 4096, 4097, 50000])
+@pytest.mark.parametrize("n", [0, 1, 2, 3, 5, 17, 100, 1023, 1024, 1025, 3000, 4095, 4096, 4097, 50000])
 def test_build_sizes_match_oracle(gsq, port, n):
     boxes = W.random_boxes(n, 100 + n) if n else np.zeros((0, 6))
     b, h = check_layout(gsq, port, boxes, 1.000123)
