@@ -31,7 +31,7 @@ struct MixedStats
 // warp replays the parked lanes' queues in order in FP64, converged.  The FP64 state
 // therefore evolves through exactly the reference's checkCandidate calls on
 // exactly the reference's candidates.  Finished lanes take the next point from
-// the queue of Morton-ordered points with one warp-aggregated atomic.
+// the queue of Morton-ordered points, which a warp takes 32 at a time.
 //
 // STK is the traversal stack depth (the reference's 64, or 32 where every
 // tree is shallow enough).  MULTI: the points belong to several meshes (point
@@ -179,18 +179,36 @@ __global__ void __launch_bounds__(128, 5) k_sdf_mixed(const NodeRec64* __restric
     if(cur < 0 && cur != BARRIER) cur = pop();
   };
 
+  // Work comes in runs of 32 consecutive (Morton-ordered) points per warp,
+  // [cb, ce): the lanes of a warp work on neighbouring points, which share
+  // most of their node and leaf records (16M uniform points: 468 instead of
+  // 482 ms; runs of 64 lost more near the surface than they gained).
+  int cb = 0, ce = 0;
   while(true)
   {
     const unsigned want = __ballot_sync(FULL, mode == M_IDLE && open);
     if(want)
     {
       const int leader = __ffs(want) - 1;
-      int base = 0;
-      if(lane == leader) base = atomicAdd(work, __popc(want));
-      base = __shfl_sync(FULL, base, leader);
+      const int nw = __popc(want), avail = ce - cb;
+      int nb = 0;
+      if(avail < nw)  // the run's rest, then a new run of 32 (nw - avail <= 32)
+      {
+        if(lane == leader) nb = atomicAdd(work, 32);
+        nb = __shfl_sync(FULL, nb, leader);
+      }
+      const int rk = __popc(want & lt_mask);
+      const int tk = (rk < avail) ? cb + rk : nb + (rk - avail);
+      if(avail < nw)
+      {
+        cb = nb + (nw - avail);
+        ce = nb + 32;
+      }
+      else
+        cb += nw;
       if(mode == M_IDLE && open)
       {
-        const int t = base + __popc(want & lt_mask);
+        const int t = tk;
         if(t < m)
         {
           idx = order ? __ldg(order + t) : t;
