@@ -93,9 +93,11 @@ __global__ void k_cpq_codes(const double* __restrict__ q, int m, const double* b
   uint32_t u[3];
   for(int d = 0; d < 3; ++d)
   {
+    // the object points' box grown by a quarter of its extent on every side,
+    // so that queries just outside it keep distinct codes
     const double ext = b[3 + d] - b[d];
-    const double sc = (ext > 0.0) ? 1.0 / ext : 0.0;
-    u[d] = (uint32_t)(int)fmin(fmax((q[3 * (size_t)i + d] - b[d]) * sc * 1024.0, 0.0), 1023.0);
+    const double sc = (ext > 0.0) ? 1.0 / (1.5 * ext) : 0.0;
+    u[d] = (uint32_t)(int)fmin(fmax((q[3 * (size_t)i + d] - (b[d] - 0.25 * ext)) * sc * 1024.0, 0.0), 1023.0);
   }
   auto spread = [](uint32_t x) {
     x = (x | (x << 16)) & 0xFF0000FFu;

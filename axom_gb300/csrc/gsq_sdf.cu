@@ -146,6 +146,20 @@ __global__ void k_leaf_records(const int* __restrict__ perm, int nleaves, const 
 
 // 30-bit Morton code of each query point in the given box (processing order
 // only; results do not depend on it).
+// The frame of the points' processing order: the mesh box grown by a quarter of
+// its extent on every side (points just outside the mesh, common in uniform
+// query sets, keep distinct codes instead of piling up on the box faces;
+// 16M points in the 1.2x box: 460 instead of 467 ms), and the inverse extent.
+inline void query_code_frame(const double* b, double* lo, double* sc)
+{
+  for(int d = 0; d < 3; ++d)
+  {
+    const double ext = b[3 + d] - b[d];
+    lo[d] = b[d] - 0.25 * ext;
+    sc[d] = (ext > 0.0) ? 1.0 / (1.5 * ext) : 0.0;
+  }
+}
+
 __global__ void k_query_codes(QueryPts qp, int m, double lx, double ly, double lz, double sx, double sy, double sz,
                               uint32_t* __restrict__ codes)
 {
@@ -245,13 +259,8 @@ int sdf_query_order(const gsq_sdf* h, const QueryPts& qp, int m, uint32_t* keys[
 {
   *order = nullptr;
   if(!h->opts.sort_queries || m <= 1) return GSQ_OK;
-  const double* b = bvh_dev(h->bvh)->bounds;
-  double sc[3];
-  for(int d = 0; d < 3; ++d)
-  {
-    const double ext = b[3 + d] - b[d];
-    sc[d] = (ext > 0.0) ? 1.0 / ext : 0.0;
-  }
+  double b[3], sc[3];
+  query_code_frame(bvh_dev(h->bvh)->bounds, b, sc);
   count_launch();
   k_query_codes<<<grid_for(m, 256), 256, 0, s>>>(qp, m, b[0], b[1], b[2], sc[0], sc[1], sc[2], keys[0]);
   const int which = radix_sort_pairs(keys, vals, m, 30, true, s, h->d_err);
@@ -503,13 +512,8 @@ int sdf_eval_impl(const gsq_sdf* hc, const double* qx, const double* qy, const d
     }
     uint32_t* keys[2] = {ob4, ob4 + m};
     int* vals[2] = {reinterpret_cast<int*>(ob4 + 2 * (size_t)m), reinterpret_cast<int*>(ob4 + 3 * (size_t)m)};
-    const double* b = B->bounds;
-    double sc[3];
-    for(int d = 0; d < 3; ++d)
-    {
-      const double ext = b[3 + d] - b[d];
-      sc[d] = (ext > 0.0) ? 1.0 / ext : 0.0;
-    }
+    double b[3], sc[3];
+    query_code_frame(B->bounds, b, sc);
     count_launch();
     k_query_codes<<<grid_for(m, 256), 256, 0, s>>>(qp, m, b[0], b[1], b[2], sc[0], sc[1], sc[2], keys[0]);
     char* sw = take(sort_bytes);
@@ -683,13 +687,8 @@ int gsq_sdf_eval_noalloc(const gsq_sdf* hc, const double* qx, const double* qy, 
   const int* order = nullptr;
   if(h->opts.sort_queries && m > 1)
   {
-    const double* b = B->bounds;
-    double sc[3];
-    for(int d = 0; d < 3; ++d)
-    {
-      const double ext = b[3 + d] - b[d];
-      sc[d] = (ext > 0.0) ? 1.0 / ext : 0.0;
-    }
+    double b[3], sc[3];
+    query_code_frame(B->bounds, b, sc);
     count_launch();
     k_query_codes<<<grid_for(m, 256), 256, 0, s>>>(qp, m, b[0], b[1], b[2], sc[0], sc[1], sc[2], keys[0]);
     const int which = radix_sort_pairs_prealloc(keys, vals, m, 30, true, sort_work,

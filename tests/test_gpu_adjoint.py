@@ -204,6 +204,8 @@ def point_triangle_distance(p, a, b, c):
     def inside(x, u, v, w):
         return np.einsum("ij,ij->i", np.cross(v - u, x - u), n) >= 0
     ins = inside(proj, a, b, c) & inside(proj, b, c, a) & inside(proj, c, a, b)
+    # a degenerate triangle has no face: its distance is the edges'
+    ins &= nn > 1e-12 * np.linalg.norm(b - a, axis=1) * np.linalg.norm(c - a, axis=1)
     d = np.minimum(np.minimum(seg(p, a, b), seg(p, b, c)), seg(p, c, a))
     return np.where(ins, np.abs(h), d)
 
@@ -246,3 +248,34 @@ def test_backward_with_forward_triangles(gsq, case):
     r = sd.backward(case["qd"][:n].contiguous(), g[:n].contiguous())
     assert np.array_equal(h[0].view(np.int64), r[0].cpu().numpy().view(np.int64))
     assert np.array_equal(h[1].view(np.int64), r[1].cpu().numpy().view(np.int64))
+
+
+@pytest.mark.parametrize("name", ["sdf_uvsphere", "sdf_ico3_open", "sdf_ico3_unsigned", "sdf_quad12"])
+@pytest.mark.parametrize("precision", ["mixed", "fp64"])
+def test_triangle_forms_on_golden_meshes(gsq, name, precision):
+    """On the reference-generated fixtures (quads, an open and an unsigned
+    mesh among them): gsq_sdf_eval_tri's distances equal the reference's bit
+    for bit, each point lies |d| from its returned triangle (quad cell c split
+    into (0, 1, 2) = 2c and (0, 2, 3) = 2c + 1), and gsq_sdf_backward_tri
+    equals gsq_sdf_backward bit for bit."""
+    from conftest import assert_bits_equal, golden
+    g = golden(name)
+    sd = gsq.SignedDistance(g["vertices"], g["cells"], bool(g["watertight"]), bool(g["sign"]),
+                            precision=axom_gb300.PRECISION_MIXED if precision == "mixed" else axom_gb300.PRECISION_FP64)
+    q = np.ascontiguousarray(g["queries"])
+    d, tri = sd.compute_distances_tri(q)
+    assert_bits_equal(d, g["dist"], "distance")
+    cells, v = np.asarray(g["cells"]), np.asarray(g["vertices"])
+    assert (tri >= 0).all()
+    if cells.shape[1] == 3:
+        f = cells[tri]
+    else:
+        c, sub = cells[tri >> 1], tri & 1
+        f = np.where(sub[:, None] == 0, c[:, [0, 1, 2]], c[:, [0, 2, 3]])
+    dt = point_triangle_distance(q, v[f[:, 0]], v[f[:, 1]], v[f[:, 2]])
+    np.testing.assert_allclose(dt, np.abs(d), rtol=1e-9, atol=1e-13)
+    w = W.rng(7).uniform(0.0, 1.0, size=len(q))
+    a = sd.backward(q, 2.0 * w * d)
+    b = sd.backward(q, 2.0 * w * d, dist=d, triangles=tri)
+    assert np.array_equal(a[0].view(np.int64), b[0].view(np.int64))
+    assert np.array_equal(a[1].view(np.int64), b[1].view(np.int64))
