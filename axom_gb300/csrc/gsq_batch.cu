@@ -297,9 +297,11 @@ __global__ void __launch_bounds__(BT) k_b_point_keys(const double* __restrict__ 
   uint32_t u[3];
   for(int d = 0; d < 3; ++d)
   {
+    // the mesh's box grown by a quarter of its extent on every side (as the
+    // single-mesh query orders its points)
     const double ext = b[3 + d] - b[d];
-    const double sc = (ext > 0.0) ? 1.0 / ext : 0.0;
-    const double f = fmin(fmax((q[3 * (size_t)i + d] - b[d]) * sc * 1024.0, 0.0), 1023.0);
+    const double sc = (ext > 0.0) ? 1.0 / (1.5 * ext) : 0.0;
+    const double f = fmin(fmax((q[3 * (size_t)i + d] - (b[d] - 0.25 * ext)) * sc * 1024.0, 0.0), 1023.0);
     u[d] = (uint32_t)(int)f;
   }
   const uint32_t code = lbvh::spread10(u[0]) | (lbvh::spread10(u[1]) << 1) | (lbvh::spread10(u[2]) << 2);
