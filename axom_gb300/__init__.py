@@ -75,6 +75,7 @@ class BatchOpts(C.Structure):
 # (name, restype, argtypes) of every entry point declared in include/gsq.h
 SIGNATURES = [
     ("gsq_last_error", C.c_char_p, []),
+    ("gsq_selftest_bounded_wait", C.c_int, [_vp]),
     ("gsq_version", C.c_char_p, []),
     ("gsq_kernel_launches", C.c_int64, []),
     ("gsq_free", C.c_int, [_vp]),

@@ -281,6 +281,34 @@ __global__ void __launch_bounds__(SCAN_THREADS) k_scan_apply(const int* __restri
 }
 }  // namespace
 
+// Self-test of the bounded waits: one block runs a onesweep pass on tile 1
+// of a two-tile input while tile 0 is never processed, so its look-back waits
+// for a flag nothing sets.  After SPIN_LIMIT polls without progress the block
+// sets DEVERR_WAIT, finishes its pass (its scatter stays inside the output)
+// and the call reports GSQ_ERR_DEVICE; the context stays usable.
+int sort_wait_selftest(cudaStream_t s)
+{
+  const int n = 2 * TILE;
+  Scratch buf;
+  const size_t words = 4 * (size_t)n + (size_t)2 * RADIX + 64;
+  GSQ_CUDA_TRY(buf.alloc(sizeof(unsigned) * words, s));
+  unsigned* w = buf.as<unsigned>();
+  GSQ_CUDA_TRY(cudaMemsetAsync(w, 0, sizeof(unsigned) * words, s));
+  uint32_t* kin = w;
+  uint32_t* kout = w + n;
+  int* vout = reinterpret_cast<int*>(w + 2 * (size_t)n);
+  unsigned* offsets = w + 3 * (size_t)n;                  // RADIX zero digit offsets
+  unsigned* lookback = offsets + RADIX;                    // two tiles x RADIX, never published for tile 0
+  int* tile_counter = reinterpret_cast<int*>(w + 4 * (size_t)n);  // words after the look-back area
+  int* err = tile_counter + 8;
+  const int one = 1;  // the block takes tile 1
+  GSQ_CUDA_TRY(cudaMemcpyAsync(tile_counter, &one, sizeof(int), cudaMemcpyHostToDevice, s));
+  count_launch();
+  k_onesweep<<<1, THREADS, 0, s>>>(kin, nullptr, 1, kout, vout, n, 0, offsets, lookback, tile_counter, err);
+  GSQ_CUDA_TRY(cudaGetLastError());
+  return check_device_error(err, s, "sort wait self-test");
+}
+
 int radix_sort_pairs(uint32_t* keys[2], int* vals[2], int n, int end_bit, bool vals_iota, cudaStream_t s, int* d_err)
 {
   if(n <= 0) return 0;
@@ -378,3 +406,8 @@ int exclusive_scan(const int* d_in, int* d_out, int m, long long* d_total, cudaS
 }
 
 }  // namespace gsq
+
+extern "C" int gsq_selftest_bounded_wait(void* stream)
+{
+  return gsq::sort_wait_selftest(static_cast<cudaStream_t>(stream));
+}

@@ -43,8 +43,8 @@ BATCH_MESHES = 512
 # profiles/k_sdf_mixed_level8_uniform_1M.md (1,048,576 uniform points of the
 # same mesh): DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) and L2
 # bytes (lts__t_sectors.sum x 32); the bench scales them by its point count.
-MIXED_DRAM_BYTES_PER_POINT = (2.335463e9 + 0.588246e9) / 1048576
-MIXED_L2_BYTES_PER_POINT = 2939739629 * 32 / 1048576
+MIXED_DRAM_BYTES_PER_POINT = (2.303622e9 + 0.580745e9) / 1048576
+MIXED_L2_BYTES_PER_POINT = 2884381452 * 32 / 1048576
 BATCH_SEED = 5
 # The 100,000-box workload: boxes from seed 1, query boxes from seed 2.
 C1_BOXES = 100_000

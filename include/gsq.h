@@ -63,6 +63,15 @@ typedef struct gsq_sdf gsq_sdf;
 /* Message of the last failed call on this thread ("" if none). */
 const char* gsq_last_error(void);
 
+/* Self-test of the kernels' bounded waits (no reference counterpart): runs
+ * one block of the radix sort's onesweep pass on the second tile of a
+ * two-tile input while the first tile is never processed, so that its
+ * decoupled look-back waits for a flag nothing sets.  The wait gives up after
+ * its poll limit (about a second), the kernel finishes without writing
+ * outside its buffers, and the call returns GSQ_ERR_DEVICE with "expired
+ * bounded wait" in gsq_last_error(); the CUDA context stays usable. */
+int gsq_selftest_bounded_wait(void* stream);
+
 /* Library version string. */
 const char* gsq_version(void);
 
