@@ -614,7 +614,11 @@ def run_gsq(args, world, rank, local):
         "dtype": "f32 traversal + f64 refine" if args.precision == "mixed" else "f64", "data": "synthetic",
         "config": workload_config(args, f),
         "fp64": fp64,
-        "build_ms": {"value": statistics.median(build_ms), "boxes": int(f.shape[0]), "runs": len(build_ms)},
+        "build_ms": {"value": statistics.median(build_ms), "boxes": int(f.shape[0]), "runs": len(build_ms),
+                     "roofline": {"bound": "hbm", "unit": "GB/s", "peak": hbm, "peak_kind": hbm_kind,
+                                  "algorithmic_bytes_per_box": BUILD_BYTES_PER_BOX,
+                                  "achieved": BUILD_BYTES_PER_BOX * f.shape[0] / (statistics.median(build_ms) / 1e3) / 1e9,
+                                  "frac": BUILD_BYTES_PER_BOX * f.shape[0] / (statistics.median(build_ms) / 1e3) / 1e9 / hbm}},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
                      "traffic": MIXED_DRAM_BYTES_PER_POINT * m if args.precision == "mixed" else None,
                      "traffic_note": "ncu DRAM bytes per point on a 1,048,576-point launch, scaled to this launch "
