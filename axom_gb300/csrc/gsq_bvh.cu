@@ -854,11 +854,16 @@ struct FindCache
   std::mutex busy;
   void* work = nullptr;
   size_t work_bytes = 0;
+  void* cand = nullptr;  // the candidates of a find with host outputs, on the device
+  size_t cand_bytes = 0;
   long long* host = nullptr;  // pinned: [0] total, [1] error word
   cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
   void release()
   {
     if(work) cudaFree(work);
+    if(cand) cudaFree(cand);
+    cand = nullptr;
+    cand_bytes = 0;
     if(host) cudaFreeHost(host);
     for(auto& e : ev)
       if(e) cudaEventDestroy(e);
@@ -941,13 +946,11 @@ int find_impl(const gsq_bvh* h, const double* a, const double* b, int32_t m, int
   InBuf qa_buf, qb_buf;
   GSQ_CUDA_TRY(qa_buf.stage(a, sizeof(double) * width * (size_t)m, s));
   if(KIND == Q_RAYS) GSQ_CUDA_TRY(qb_buf.stage(b, sizeof(double) * 3 * (size_t)m, s));
-  OutBuf off_buf, cnt_buf;
-  GSQ_CUDA_TRY(off_buf.prepare(offsets, sizeof(int) * (size_t)m, s));
-  GSQ_CUDA_TRY(cnt_buf.prepare(counts, sizeof(int) * (size_t)m, s));
   // scratch: the handle's cache, or (when another thread holds it) the call's own
   const size_t keep_bytes = (sizeof(int) * FIND_CAP * (size_t)std::max(m, 1) + 255) & ~size_t(255);
   const size_t scan_bytes = (exclusive_scan_work_bytes(m) + 255) & ~size_t(255);
-  const size_t need = keep_bytes + scan_bytes + 256;
+  const size_t csr_bytes = dev_out ? 0 : 2 * align256(sizeof(int) * (size_t)std::max(m, 1));  // host offsets, counts
+  const size_t need = keep_bytes + scan_bytes + 256 + csr_bytes;
   FindCache& fc = h->fc;
   std::unique_lock<std::mutex> lock(fc.busy, std::try_to_lock);
   const bool cached = lock.owns_lock();
@@ -984,6 +987,10 @@ int find_impl(const gsq_bvh* h, const double* a, const double* b, int32_t m, int
   int* keep = reinterpret_cast<int*>(work);
   void* scan_work = work + keep_bytes;
   long long* d_tot = reinterpret_cast<long long*>(work + keep_bytes + scan_bytes);
+  char* csr = csr_bytes ? work + keep_bytes + scan_bytes + 256 : nullptr;
+  OutBuf off_buf, cnt_buf;
+  GSQ_CUDA_TRY(off_buf.prepare(offsets, sizeof(int) * (size_t)m, s, csr));
+  GSQ_CUDA_TRY(cnt_buf.prepare(counts, sizeof(int) * (size_t)m, s, csr ? csr + csr_bytes / 2 : nullptr));
   QueryArgs qa {static_cast<const double*>(qa_buf.dev), static_cast<const double*>(qb_buf.dev), h->tol};
   int* d_cnt = static_cast<int*>(cnt_buf.dev);
   int* d_off = static_cast<int*>(off_buf.dev);
@@ -1015,8 +1022,25 @@ int find_impl(const gsq_bvh* h, const double* a, const double* b, int32_t m, int
     if(rc) return rc;
   }
   if(total > INT_MAX) return fail(GSQ_ERR_INVALID, "more than 2^31-1 candidates");
+  // the candidates: a new device array when the caller takes device outputs,
+  // else the cache's (grow-only) before the copy to host memory
   int* d_cand = nullptr;
-  GSQ_CUDA_TRY(cudaMalloc(&d_cand, sizeof(int) * (size_t)std::max<long long>(total, 1)));
+  const size_t cand_bytes = sizeof(int) * (size_t)std::max<long long>(total, 1);
+  const bool cand_cached = cached && !dev_out;
+  if(cand_cached)
+  {
+    if(cand_bytes > fc.cand_bytes)
+    {
+      if(fc.cand) cudaFree(fc.cand);
+      fc.cand = nullptr;
+      fc.cand_bytes = 0;
+      GSQ_CUDA_TRY(cudaMalloc(&fc.cand, cand_bytes));
+      fc.cand_bytes = cand_bytes;
+    }
+    d_cand = static_cast<int*>(fc.cand);
+  }
+  else
+    GSQ_CUDA_TRY(cudaMalloc(&d_cand, cand_bytes));
   cudaEventRecord(ev[2], s);
   if(m > 0)
   {
@@ -1037,7 +1061,7 @@ int find_impl(const gsq_bvh* h, const double* a, const double* b, int32_t m, int
     {
       e = cudaMemcpyAsync(host, d_cand, sizeof(int) * (size_t)total, cudaMemcpyDeviceToHost, s);
       if(e == cudaSuccess) e = cudaStreamSynchronize(s);
-      cudaFree(d_cand);
+      if(!cand_cached) cudaFree(d_cand);
       d_cand = nullptr;
       *candidates = host;
       if(e != cudaSuccess)
@@ -1047,12 +1071,12 @@ int find_impl(const gsq_bvh* h, const double* a, const double* b, int32_t m, int
       }
     }
   }
-  else
+  else if(dev_out)
     *candidates = d_cand;
   if(e == cudaSuccess) e = cudaStreamSynchronize(s);
   if(e != cudaSuccess)
   {
-    if(d_cand) cudaFree(d_cand);
+    if(d_cand && !cand_cached) cudaFree(d_cand);
     *candidates = nullptr;
     return cuda_fail(e, "find pass 2");
   }
