@@ -186,3 +186,28 @@ def test_mesh_self_query_broad_phase(gsq, port):
     for x, y in zip(got, want):
         assert_bits_equal(x, y, "self query")
     assert int(got[1].min()) >= 1  # every box finds at least itself
+
+
+def test_rebuilt_handle_answers_for_its_new_boxes(gsq, port):
+    """One handle rebuilt over other boxes (other counts, then the same count
+    with other coordinates, then the first set again, which replays the
+    captured build) answers box, point and ray finds for the boxes it holds:
+    the per-node key records of the box and point finds are remade after every
+    build."""
+    sets = [W.random_boxes(30_000, 31), W.random_boxes(12_000, 32), W.random_boxes(12_000, 33),
+            W.random_boxes(30_000, 31), W.random_boxes(30_000, 31)]
+    q = W.random_boxes(3_000, 34)
+    r = W.rng(35)
+    pts = r.uniform(0, 1, (3_000, 3))
+    o = r.uniform(-0.1, 1.1, (500, 3))
+    d = port.normalize_rays(r.normal(size=(500, 3)))
+    b = gsq.BVH()
+    for boxes in sets:
+        b.initialize(boxes)
+        h = port.bvh(boxes)
+        for x, y in zip(b.find_bounding_boxes(q), port.find_boxes(h, q)):
+            assert_bits_equal(np.asarray(x), y, "find boxes after a rebuild")
+        for x, y in zip(b.find_points(pts), port.find_points(h, pts)):
+            assert_bits_equal(np.asarray(x), y, "find points after a rebuild")
+        for x, y in zip(b.find_rays(o, d), port.find_rays(h, o, d)):
+            assert_bits_equal(np.asarray(x), y, "find rays after a rebuild")
