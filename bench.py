@@ -532,6 +532,16 @@ def run_gsq(args, world, rank, local):
         bvh.initialize(boxes)
         if i >= args.warmup:
             build_ms.append(bvh.last_build_ms())
+    # the SignedDistance constructor (host vertices and cells in: the copies,
+    # the cell boxes, the BVH build, the FP64 and FP32 records), wall clock
+    ctor_ms = []
+    for i in range(3):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        sd_new = G.SignedDistance(v, f, precision=prec)
+        torch.cuda.synchronize()
+        ctor_ms.append((time.perf_counter() - t0) * 1000.0)
+        del sd_new
 
     def run_steps(precision, steps, warmup):
         sd.set_precision(precision)
@@ -614,6 +624,8 @@ def run_gsq(args, world, rank, local):
         "dtype": "f32 traversal + f64 refine" if args.precision == "mixed" else "f64", "data": "synthetic",
         "config": workload_config(args, f),
         "fp64": fp64,
+        "sdf_ctor_ms": {"value": statistics.median(ctor_ms), "runs": len(ctor_ms),
+                        "note": "SignedDistance constructor from host vertices and cells, wall clock"},
         "build_ms": {"value": statistics.median(build_ms), "boxes": int(f.shape[0]), "runs": len(build_ms),
                      "roofline": {"bound": "hbm", "unit": "GB/s", "peak": hbm, "peak_kind": hbm_kind,
                                   "algorithmic_bytes_per_box": BUILD_BYTES_PER_BOX,
