@@ -88,9 +88,14 @@ __device__ __forceinline__ Fold fold_block(Fold f)
   fold_warp(f);
   if((threadIdx.x & 31) == 0) s_f[threadIdx.x >> 5] = f;
   __syncthreads();
-  Fold a = s_f[0];
-  if(threadIdx.x == 0)
-    for(int w = 1; w < (int)(blockDim.x >> 5); ++w) fold_merge(a, s_f[w]);
+  Fold a;
+  fold_init(a);
+  if(threadIdx.x < 32)
+  {
+    // the first warp merges the warps' folds (the merge is commutative)
+    if(threadIdx.x < (blockDim.x >> 5)) a = s_f[threadIdx.x];
+    fold_warp(a);
+  }
   __syncthreads();
   return a;
 }
