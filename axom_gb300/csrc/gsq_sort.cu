@@ -40,9 +40,14 @@ __device__ __forceinline__ unsigned ld_volatile(const unsigned* p)
 }
 __device__ __forceinline__ void st_volatile(unsigned* p, unsigned v) { *reinterpret_cast<volatile unsigned*>(p) = v; }
 
-__global__ void k_histogram(const uint32_t* __restrict__ keys, int n, int passes, unsigned* __restrict__ hist)
+// Digit counts of every pass (one shared histogram per block, added into
+// hist), then the exclusive prefix over the 256 digits of every pass, taken by
+// the last block to finish (`done`, zeroed with hist; blockDim.x == RADIX).
+__global__ void __launch_bounds__(RADIX) k_histogram(const uint32_t* __restrict__ keys, int n, int passes,
+                                                     unsigned* __restrict__ hist, unsigned* __restrict__ done)
 {
   __shared__ unsigned sh[4 * RADIX];
+  __shared__ bool s_last;
   for(int i = threadIdx.x; i < passes * RADIX; i += blockDim.x) sh[i] = 0;
   __syncthreads();
   for(int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
@@ -53,15 +58,16 @@ __global__ void k_histogram(const uint32_t* __restrict__ keys, int n, int passes
   __syncthreads();
   for(int i = threadIdx.x; i < passes * RADIX; i += blockDim.x)
     if(sh[i]) atomicAdd(&hist[i], sh[i]);
-}
-
-// Exclusive prefix over the 256 digits of every pass (one block of 256).
-__global__ void k_histogram_scan(unsigned* hist, int passes)
-{
-  __shared__ unsigned s[RADIX];
+  __threadfence();
+  __syncthreads();
+  if(threadIdx.x == 0) s_last = (atomicAdd(done, 1u) == gridDim.x - 1);
+  __syncthreads();
+  if(!s_last) return;
+  __threadfence();
+  unsigned* s = sh;  // reused: one pass at a time
   for(int p = 0; p < passes; ++p)
   {
-    const unsigned v = hist[p * RADIX + threadIdx.x];
+    const unsigned v = __ldcg(&hist[p * RADIX + threadIdx.x]);
     s[threadIdx.x] = v;
     __syncthreads();
     for(int off = 1; off < RADIX; off <<= 1)
@@ -322,11 +328,12 @@ int radix_sort_pairs(uint32_t* keys[2], int* vals[2], int n, int end_bit, bool v
   unsigned* hist = work.as<unsigned>();
   unsigned* lookback = hist + hist_words;
   int* tile_counter = reinterpret_cast<int*>(lookback + lb_words);
-  GSQ_CUDA_TRY(cudaMemsetAsync(hist, 0, sizeof(unsigned) * hist_words, s));
+  // hist and, in the first look-back word (free until the first pass clears
+  // the look-back area), the histogram's block counter
+  GSQ_CUDA_TRY(cudaMemsetAsync(hist, 0, sizeof(unsigned) * (hist_words + 1), s));
   const int hblocks = (int)std::min<long long>(((long long)n + 1023) / 1024, 1024);
-  k_histogram<<<hblocks, 256, 0, s>>>(keys[0], n, passes, hist);
-  k_histogram_scan<<<1, RADIX, 0, s>>>(hist, passes);
-  count_launch(2 + passes);
+  k_histogram<<<hblocks, RADIX, 0, s>>>(keys[0], n, passes, hist, lookback);
+  count_launch(1 + passes);
   int cur = 0;
   for(int p = 0; p < passes; ++p)
   {
@@ -359,11 +366,12 @@ int radix_sort_pairs_prealloc(uint32_t* keys[2], int* vals[2], int n, int end_bi
   unsigned* hist = static_cast<unsigned*>(work);
   unsigned* lookback = hist + hist_words;
   int* tile_counter = reinterpret_cast<int*>(lookback + lb_words);
-  GSQ_CUDA_TRY(cudaMemsetAsync(hist, 0, sizeof(unsigned) * hist_words, s));
+  // hist and, in the first look-back word (free until the first pass clears
+  // the look-back area), the histogram's block counter
+  GSQ_CUDA_TRY(cudaMemsetAsync(hist, 0, sizeof(unsigned) * (hist_words + 1), s));
   const int hblocks = (int)std::min<long long>(((long long)n + 1023) / 1024, 1024);
-  k_histogram<<<hblocks, 256, 0, s>>>(keys[0], n, passes, hist);
-  k_histogram_scan<<<1, RADIX, 0, s>>>(hist, passes);
-  count_launch(2 + passes);
+  k_histogram<<<hblocks, RADIX, 0, s>>>(keys[0], n, passes, hist, lookback);
+  count_launch(1 + passes);
   int cur = 0;
   for(int p = 0; p < passes; ++p)
   {
